@@ -1,0 +1,431 @@
+"""Benchmark: batched s-t connectivity on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fastcon|reference]
+                    [--config rmat24|er65536|grid4096|batched512]
+
+Default workload (rmat24): R-MAT scale 24 (16,777,216 vertices; 8 * 2^24 edge
+samples with a/b/c/d = .57/.19/.19/.05 -> average degree ~16 after
+symmetrisation and deduplication; ids permuted, seed 3), 1,024 (s, t) pairs
+among vertices of degree >= 1 (seed 4).  One step = all 1,024 queries through
+the library's batched engine.  The graph (CSR ~1 GB) is larger than L2, so no
+L2 flush is added between steps.
+
+Printed line (rank 0): value = queries/s with inputs resident in HBM (CUDA
+events on the launching stream); e2e = the same through fc_stcon_batch with
+pinned host arrays (copies inside the timed region); roofline of the
+dominant kernel; cpu_baseline = the reference's CPU path (full BFS per query,
+Graph::bfs semantics) on the host cores; plain = the plain level-synchronous
+GPU form (host-driven, alternating sides, top-down) on a sample.
+
+--impl reference times the reference's CPU path alone (rank 0) on bounded
+samples of the same workload and prints the same metric with impl=reference.
+Multi-GPU: queries do not exchange data, so N ranks run N independent
+replicas (one per GPU) and value sums them (scaling = weak).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "fast-con_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "ST-CON queries/s & GTEPS: learned+batched vs plain on 1 GB300, exact answers"
+UNIT = "queries/s"
+
+CONFIGS = {
+    "rmat24": dict(kind="rmat", scale=24, edge_samples=8 << 24, seed=3, perm_seed=3, nq=1024,
+                   qseed=4),
+    "er65536": dict(kind="er", n=65536, m=524288, seed=1, nq=64, qseed=2),
+    "grid4096": dict(kind="grid", w=4096, h=4096, p_del=0.05, del_seed=5, sc_seed=6, nq=256,
+                     qseed=7, min_manhattan=2000),
+}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read only)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x: float) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(ws, x: float) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# workload construction
+# ---------------------------------------------------------------------------
+def make_graph_gpu(fc, cfg):
+    from fastcon import graphs
+    if cfg["kind"] == "rmat":
+        G = fc.Graph.rmat(cfg["scale"], cfg["edge_samples"], seed=cfg["seed"],
+                          perm_seed=cfg["perm_seed"])
+        rp, _ = G.csr_row_ptr()
+        s, t = graphs.pairs_with_degree(np.diff(rp), cfg["nq"], seed=cfg["qseed"])
+    elif cfg["kind"] == "er":
+        u, v = graphs.er_edges(cfg["n"], cfg["m"], seed=cfg["seed"])
+        G = fc.Graph.from_edges(u, v, cfg["n"])
+        s, t = graphs.uniform_pairs(cfg["n"], cfg["nq"], seed=cfg["qseed"])
+    else:
+        n = cfg["w"] * cfg["h"]
+        G = fc.Graph.grid(cfg["w"], cfg["h"], p_del=cfg["p_del"], del_seed=cfg["del_seed"],
+                          shortcuts=graphs.grid_shortcut_count(n), sc_seed=cfg["sc_seed"])
+        s, t = graphs.grid_pairs(cfg["w"], cfg["h"], cfg["nq"], cfg["qseed"], cfg["min_manhattan"])
+    return G, s, t
+
+
+def make_graph_cpu(cfg, nthreads):
+    """Host CSR for the CPU arm, built without any GPU code (oracle C)."""
+    import oracle
+    from fastcon import graphs
+    if cfg["kind"] == "rmat":
+        n = 1 << cfg["scale"]
+        u, v = oracle.gen_rmat(cfg["scale"], cfg["edge_samples"], seed=cfg["seed"],
+                               perm_seed=cfg["perm_seed"], nthreads=nthreads)
+        rp, col = oracle.build_csr(n, u, v, nthreads=nthreads)
+        del u, v
+        s, t = graphs.pairs_with_degree(np.diff(rp), cfg["nq"], seed=cfg["qseed"])
+    elif cfg["kind"] == "er":
+        u, v = graphs.er_edges(cfg["n"], cfg["m"], seed=cfg["seed"])
+        rp, col = oracle.build_csr(cfg["n"], u, v, nthreads=nthreads)
+        s, t = graphs.uniform_pairs(cfg["n"], cfg["nq"], seed=cfg["qseed"])
+    else:
+        n = cfg["w"] * cfg["h"]
+        u, v = graphs.grid_edges(cfg["w"], cfg["h"], cfg["p_del"], cfg["del_seed"],
+                                 graphs.grid_shortcut_count(n), cfg["sc_seed"])
+        rp, col = oracle.build_csr(n, u, v, nthreads=nthreads)
+        s, t = graphs.grid_pairs(cfg["w"], cfg["h"], cfg["nq"], cfg["qseed"], cfg["min_manhattan"])
+    return rp, col, s, t
+
+
+def cpu_sample_size(cfg):
+    return {"rmat": 32, "er": 64, "grid": 32}[cfg["kind"]]
+
+
+def time_cpu_reference(rp, col, s, t, nthreads, min_seconds=10.0, max_queries=None):
+    """The reference's CPU path (one full BFS per query, Graph::bfs) on a
+    bounded sample; returns (queries/s, queries timed, seconds)."""
+    import oracle
+    nq = len(s)
+    done = 0
+    t0 = time.perf_counter()
+    chunk = max(nthreads, 1)
+    while True:
+        lo = done % nq
+        hi = min(nq, lo + chunk)
+        oracle.stcon_batch(rp, col, s[lo:hi], t[lo:hi], nthreads=nthreads)
+        done += hi - lo
+        el = time.perf_counter() - t0
+        if el >= min_seconds or (max_queries and done >= max_queries):
+            break
+    return done / el, done, el
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+def run_reference(args, cfg):
+    ws, rank, _ = dist_env()
+    if ws > 1 and rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    rp, col, s, t = make_graph_cpu(cfg, nthreads)
+    per_step = max(nthreads, cpu_sample_size(cfg))
+    rates = []
+    for i in range(args.warmup + args.steps):
+        lo = (i * per_step) % len(s)
+        idx = np.arange(lo, lo + per_step) % len(s)
+        t0 = time.perf_counter()
+        import oracle
+        oracle.stcon_batch(rp, col, s[idx], t[idx], nthreads=nthreads)
+        el = time.perf_counter() - t0
+        if i >= args.warmup:
+            rates.append((per_step, el))
+    q = sum(r[0] for r in rates)
+    el = sum(r[1] for r in rates)
+    value = q / el
+    kind = "port"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * el / len(rates),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic", "config": config_desc(args.config, cfg),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": kind,
+                         "sample": f"{per_step} of the {len(s)} queries per step, one full BFS "
+                                   f"from s per query (Graph::bfs), {nthreads} threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_desc(name, cfg):
+    d = {"workload": name}
+    if cfg["kind"] == "rmat":
+        d.update({"graph": f"R-MAT scale {cfg['scale']}, {cfg['edge_samples']} edge samples "
+                           "(edge factor 16 counted as average degree), a/b/c/d=.57/.19/.19/.05, "
+                           f"ids permuted (seed {cfg['perm_seed']})",
+                  "queries": cfg["nq"], "query_seed": cfg["qseed"],
+                  "l2": "inputs larger than L2 (CSR > 126 MB)"})
+    elif cfg["kind"] == "er":
+        d.update({"graph": f"G(n,m) n={cfg['n']} m={cfg['m']} seed {cfg['seed']}",
+                  "queries": cfg["nq"], "l2": "graph fits in L2 (small config)"})
+    else:
+        d.update({"graph": f"{cfg['w']}x{cfg['h']} grid, {cfg['p_del']:.0%} edges deleted, "
+                           "0.01% shortcuts", "queries": cfg["nq"],
+                  "l2": "inputs larger than L2"})
+    return d
+
+
+def run_fastcon(args, cfg):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import fastcon as fc
+    import oracle
+
+    G, s, t = make_graph_gpu(fc, cfg)
+    nq = len(s)
+    stream = torch.cuda.current_stream()
+    opt = fc.make_opts(sched=fc.SCHED_HEURISTIC, engine=fc.ENGINE_BATCHED,
+                       stream=stream.cuda_stream)
+    d_s = torch.from_numpy(s).cuda()
+    d_t = torch.from_numpy(t).cuda()
+    d_c = torch.empty(nq, dtype=torch.int32, device="cuda")
+    d_h = torch.empty(nq, dtype=torch.int32, device="cuda")
+
+    def step():
+        fc.stcon_batch_device(G, d_s.data_ptr(), d_t.data_ptr(), nq, d_c.data_ptr(),
+                              d_h.data_ptr(), opts=opt)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    # correctness of this very workload on a sample (oracle, host cores)
+    hops_gpu = d_h.cpu().numpy()
+    nthreads = os.cpu_count() or 1
+    rp, col = G.csr()
+    samp = np.arange(0, nq, max(1, nq // 16))
+    _, want, _ = oracle.stcon_batch(rp, col, s[samp], t[samp], nthreads=nthreads)
+    exact = bool((hops_gpu[samp] == want).all())
+
+    clocks = ClockSampler(local)
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(ws, ms)
+    total_q = sum_over_ranks(ws, float(nq * args.steps))
+    value = total_q / (ms / 1000.0)
+
+    # per-kernel split and algorithmic bytes (same workload, stats on)
+    kms = np.zeros(2)
+    kbytes = np.zeros(2)
+    ins = 0
+    st = None
+    for _ in range(args.steps):
+        st = fc.stcon_batch_device(G, d_s.data_ptr(), d_t.data_ptr(), nq, d_c.data_ptr(),
+                                   d_h.data_ptr(), opts=opt, stats=True)
+        kms += np.array(st["kernel_ms"])
+        kbytes += np.array(st["kernel_alg_bytes"])
+        ins += st["edges_inspected"]
+    kms /= args.steps
+    kbytes /= args.steps
+    dom = int(np.argmax(kms))
+    peak, peak_src = peaks()
+    achieved = (kbytes[dom] / 1e9) / (kms[dom] / 1e3) if kms[dom] > 0 else 0.0
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None,
+                "kernel": ["k_batched", "k_persistent"][dom],
+                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "kernel_ms": kms.tolist(), "kernel_alg_bytes": kbytes.tolist(),
+                "escalated_queries": st["escalated"]}
+
+    # e2e: host arrays (pinned), copies inside the timed region
+    hs = torch.from_numpy(s).pin_memory().numpy()
+    ht = torch.from_numpy(t).pin_memory().numpy()
+    e2e_opt = fc.make_opts(sched=fc.SCHED_HEURISTIC, engine=fc.ENGINE_BATCHED)
+    fc.stcon_batch(G, hs, ht, opts=e2e_opt)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        conn, hops = fc.stcon_batch(G, hs, ht, opts=e2e_opt)
+    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(ws, e2e_s)
+    e2e = {"value": total_q / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * 4 * nq,
+           "d2h_bytes_per_step": 2 * 4 * nq}
+    exact = exact and bool((hops == hops_gpu).all())
+
+    # plain level-synchronous form on a sample
+    plain_n = min(nq, 128 if cfg["kind"] != "grid" else 16)
+    popt = fc.make_opts(sched=fc.SCHED_PLAIN, engine=fc.ENGINE_HOSTLOOP)
+    t0 = time.perf_counter()
+    pc, ph = fc.stcon_batch(G, s[:plain_n], t[:plain_n], opts=popt)
+    plain_s = time.perf_counter() - t0
+    exact = exact and bool((ph == hops_gpu[:plain_n]).all())
+    plain = {"value": plain_n / plain_s, "unit": UNIT, "sample": plain_n,
+             "form": "host loop, one launch per level, alternating sides, top-down"}
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if ws == 1:
+            rate, done, el = time_cpu_reference(rp, col, s, t, nthreads, min_seconds=10.0,
+                                                max_queries=4 * nthreads)
+            cpu = {"value": rate, "unit": UNIT, "cores": nthreads, "kind": "port",
+                   "sample": f"{done} queries of the workload ({el:.1f} s), one full BFS from s "
+                             "per query (Graph::bfs restated in oracle/fc_oracle.c)"}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": dict(config_desc(args.config, cfg), engine="batched",
+                           sched="heuristic", parallelism=f"replicas{ws}"),
+            "exact": exact,
+            "gteps_inspected": ins / args.steps / (ms / args.steps / 1000.0) / 1e9,
+            "edges_inspected_per_step": ins / args.steps,
+            "plain": plain,
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": 2 * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fastcon", choices=["fastcon", "reference"])
+    ap.add_argument("--config", default="rmat24", choices=sorted(CONFIGS))
+    args = ap.parse_args()
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        import oracle
+        oracle.build()
+        run_reference(args, cfg)
+    else:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location(
+            "fastcon_build", os.path.join(ROOT, "fast-con_gb300", "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+        import oracle
+        oracle.build()
+        run_fastcon(args, cfg)
+
+
+if __name__ == "__main__":
+    main()

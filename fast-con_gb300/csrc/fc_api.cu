@@ -1,0 +1,718 @@
+// fc_api.cu -- the extern "C" boundary (include/fastcon.h): graph handles,
+// edge-list files, argument checks, dispatch to the engines.
+#include <algorithm>
+#include <cerrno>
+#include <climits>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "fastcon.h"
+#include "fc_engine.h"
+#include "fc_ingest.h"
+#include "fc_internal.cuh"
+
+struct fc_graph {
+    int device;
+    int32_t nv;
+    int64_t ne;
+    int directed;
+    int32_t *row_ptr, *col;    // forward CSR
+    int32_t *rrow_ptr, *rcol;  // reverse CSR (same pointers when undirected)
+};
+
+namespace {
+
+using fc::set_error;
+
+int validate_ptr(const void *p, const char *name)
+{
+    if (!p) {
+        set_error("%s is NULL", name);
+        return FC_ERR_INVALID;
+    }
+    return FC_OK;
+}
+
+fc::GraphPairH pair_of(const fc_graph *g)
+{
+    fc::GraphPairH p;
+    p.fwd.row_ptr = g->row_ptr;
+    p.fwd.col = g->col;
+    p.fwd.nv = g->nv;
+    p.fwd.pad_ = 0;
+    p.fwd.ne = g->ne;
+    p.rev.row_ptr = g->rrow_ptr;
+    p.rev.col = g->rcol;
+    p.rev.nv = g->nv;
+    p.rev.pad_ = 0;
+    p.rev.ne = g->ne;
+    return p;
+}
+
+__global__ void k_csr_to_reverse_coo(const int32_t *row_ptr, const int32_t *col, int nv,
+                                     int32_t *src, int32_t *dst)
+{
+    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nv; u += gridDim.x * blockDim.x)
+        for (int j = row_ptr[u]; j < row_ptr[u + 1]; ++j) {
+            src[j] = col[j];
+            dst[j] = u;
+        }
+}
+
+// Reverse CSR of a directed graph, same multiset of edges.
+int build_reverse(fc_graph *g, cudaStream_t st)
+{
+    int32_t *s = nullptr, *d = nullptr;
+    FC_CUDA_TRY(cudaMalloc(&s, sizeof(int32_t) * (size_t)std::max<int64_t>(1, g->ne)));
+    FC_CUDA_TRY(cudaMalloc(&d, sizeof(int32_t) * (size_t)std::max<int64_t>(1, g->ne)));
+    int grid = (g->nv + 255) / 256;
+    if (grid > 152 * 32) grid = 152 * 32;
+    k_csr_to_reverse_coo<<<grid, 256, 0, st>>>(g->row_ptr, g->col, g->nv, s, d);
+    long long ne2 = 0;
+    int rc = fc::ingest_device_edges(
+        s, d, g->ne, g->nv, FC_INGEST_DIRECTED | FC_INGEST_KEEP_LOOPS | FC_INGEST_KEEP_DUPS,
+        &g->rrow_ptr, &g->rcol, &ne2, st);
+    cudaFree(s);
+    cudaFree(d);
+    return rc;
+}
+
+fc_graph *new_graph(int nv, int directed)
+{
+    fc_graph *g = (fc_graph *)calloc(1, sizeof(fc_graph));
+    if (!g) return nullptr;
+    cudaGetDevice(&g->device);
+    g->nv = nv;
+    g->directed = directed;
+    return g;
+}
+
+int finish_graph(fc_graph *g, cudaStream_t st)
+{
+    if (g->directed) {
+        int rc = build_reverse(g, st);
+        if (rc) return rc;
+    } else {
+        g->rrow_ptr = g->row_ptr;
+        g->rcol = g->col;
+    }
+    return FC_OK;
+}
+
+int from_device_edges(const int32_t *d_src, const int32_t *d_dst, int64_t n, int32_t nv, int flags,
+                      fc_graph **out, cudaStream_t st)
+{
+    fc_graph *g = new_graph(nv, (flags & FC_INGEST_DIRECTED) ? 1 : 0);
+    if (!g) return FC_ERR_OOM;
+    long long ne = 0;
+    int rc = fc::ingest_device_edges(d_src, d_dst, n, nv, flags, &g->row_ptr, &g->col, &ne, st);
+    if (rc == FC_OK) {
+        g->ne = ne;
+        rc = finish_graph(g, st);
+    }
+    if (rc != FC_OK) {
+        fc_graph_free(g);
+        return rc;
+    }
+    *out = g;
+    return FC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Edge-list files.  Formats and conventions follow the reference readers:
+//   SNAP            load_graph (S/load_graph.c:20-104): '#' comment header,
+//                   "# Nodes: N Edges: M", then "u v" per line, raw ids;
+//                   readGraphSnap (K/Util/readGraphSTD.cpp:128-145) renumbers ids
+//                   by first appearance (relabel = 1).
+//   MatrixMarket    "%%MatrixMarket ... [symmetric]", size line, 1-based pairs
+//                   (K/Util/readGraphSTD.cpp:57-75).
+//   DIMACS9         "p sp N M" and "a u v w" arcs, 1-based (K/Util/readGraphSTD.cpp:78-99).
+//   DIMACS10/METIS  "N M [fmt]" then one line of 1-based neighbours per vertex
+//                   (K/Util/readGraphSTD.cpp:101-125).
+// The vertex count is the declared one, raised to max id + 1 if an id exceeds it.
+// ---------------------------------------------------------------------------
+struct Parsed {
+    std::vector<int32_t> src, dst;
+    long long nv = 0;
+    int file_directed = -1;
+};
+
+inline bool is_digit(char c) { return c >= '0' && c <= '9'; }
+
+// parse a (possibly signed) integer at p within [p, e); returns false if none
+inline bool parse_int(const char *&p, const char *e, long long &out)
+{
+    while (p < e && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
+    if (p >= e) return false;
+    bool neg = false;
+    if (*p == '-') {
+        neg = true;
+        ++p;
+    }
+    if (p >= e || !is_digit(*p)) return false;
+    long long v = 0;
+    while (p < e && is_digit(*p)) {
+        v = v * 10 + (*p - '0');
+        if (v > (1ll << 40)) return false;
+        ++p;
+    }
+    out = neg ? -v : v;
+    return true;
+}
+
+int parse_file(const char *path, int relabel, Parsed &P)
+{
+    FILE *f = fopen(path, "rb");
+    if (!f) {
+        set_error("cannot open %s: %s", path, strerror(errno));
+        return FC_ERR_IO;
+    }
+    std::string buf;
+    if (fseek(f, 0, SEEK_END) == 0) {
+        long sz = ftell(f);
+        if (sz > 0) {
+            buf.resize((size_t)sz);
+            fseek(f, 0, SEEK_SET);
+            if (fread(&buf[0], 1, (size_t)sz, f) != (size_t)sz) {
+                fclose(f);
+                set_error("cannot read %s", path);
+                return FC_ERR_IO;
+            }
+        }
+    }
+    fclose(f);
+    const char *p = buf.data(), *end = buf.data() + buf.size();
+    int fmt = 0;  // 1 snap, 2 mm, 3 dimacs9, 4 dimacs10
+    long long declared_nodes = -1, maxid = -1;
+    bool header_done = false, mm_size = false;
+    long long d10_line = 0;
+    std::unordered_map<long long, int32_t> idmap;
+    auto map_id = [&](long long id) -> long long {
+        auto it = idmap.find(id);
+        if (it != idmap.end()) return it->second;
+        int32_t nid = (int32_t)idmap.size();
+        idmap.emplace(id, nid);
+        return nid;
+    };
+    auto push = [&](long long a, long long b) -> bool {
+        if (a < 0 || b < 0 || a > INT_MAX || b > INT_MAX) return false;
+        P.src.push_back((int32_t)a);
+        P.dst.push_back((int32_t)b);
+        if (a > maxid) maxid = a;
+        if (b > maxid) maxid = b;
+        return true;
+    };
+    while (p < end) {
+        const char *le = (const char *)memchr(p, '\n', (size_t)(end - p));
+        if (!le) le = end;
+        const char *q = p;
+        while (q < le && (*q == ' ' || *q == '\t')) ++q;
+        const char *line = q;
+        p = le + 1;
+        if (q >= le || *q == '\r') continue;
+        if (fmt == 0) {
+            if (*q == '#')
+                fmt = 1;
+            else if (le - q >= 14 && memcmp(q, "%%MatrixMarket", 14) == 0)
+                fmt = 2;
+            else if (*q == 'c' || *q == 'p')
+                fmt = 3;
+            else if (*q == '%' || is_digit(*q))
+                fmt = 4;
+            else {
+                set_error("%s: unrecognised graph format", path);
+                return FC_ERR_FORMAT;
+            }
+        }
+        std::string lstr;
+        if (fmt == 1) {
+            if (*q == '#') {
+                lstr.assign(line, le);
+                if (lstr.find("Undirected") != std::string::npos)
+                    P.file_directed = 0;
+                else if (lstr.find("Directed") != std::string::npos && P.file_directed < 0)
+                    P.file_directed = 1;
+                size_t k = lstr.find("Nodes:");
+                if (k != std::string::npos) {
+                    long long a = -1, b = -1;
+                    if (sscanf(lstr.c_str() + k, "Nodes: %lld Edges: %lld", &a, &b) >= 1)
+                        declared_nodes = a;
+                }
+                continue;
+            }
+            long long a, b;
+            if (!parse_int(q, le, a)) continue;
+            if (!parse_int(q, le, b) || a < 0 || b < 0) {
+                set_error("%s: malformed edge line", path);
+                return FC_ERR_FORMAT;
+            }
+            if (relabel) {
+                a = map_id(a);
+                b = map_id(b);
+            }
+            if (!push(a, b)) {
+                set_error("%s: vertex id out of range", path);
+                return FC_ERR_FORMAT;
+            }
+        } else if (fmt == 2) {
+            if (*q == '%') {
+                lstr.assign(line, le);
+                if (lstr.compare(0, 14, "%%MatrixMarket") == 0)
+                    P.file_directed = lstr.find("symmetric") != std::string::npos ? 0 : 1;
+                continue;
+            }
+            long long a, b, c;
+            if (!mm_size) {
+                if (!parse_int(q, le, a)) continue;
+                if (!parse_int(q, le, b) || !parse_int(q, le, c)) {
+                    set_error("%s: malformed MatrixMarket size line", path);
+                    return FC_ERR_FORMAT;
+                }
+                declared_nodes = a;
+                mm_size = true;
+                continue;
+            }
+            if (!parse_int(q, le, a)) continue;
+            if (!parse_int(q, le, b) || a < 1 || b < 1 || !push(a - 1, b - 1)) {
+                set_error("%s: malformed MatrixMarket entry", path);
+                return FC_ERR_FORMAT;
+            }
+        } else if (fmt == 3) {
+            if (*q == 'p') {
+                lstr.assign(line, le);
+                char w1[64], w2[64];
+                long long a = -1, b = -1;
+                if (sscanf(lstr.c_str(), "%63s %63s %lld %lld", w1, w2, &a, &b) == 4) declared_nodes = a;
+                continue;
+            }
+            if (*q != 'a') continue;
+            ++q;
+            long long a, b;
+            if (!parse_int(q, le, a) || !parse_int(q, le, b) || a < 1 || b < 1 || !push(a - 1, b - 1)) {
+                set_error("%s: malformed DIMACS arc", path);
+                return FC_ERR_FORMAT;
+            }
+        } else {
+            if (*q == '%') continue;
+            long long a, b, c;
+            if (!header_done) {
+                if (!parse_int(q, le, a)) continue;
+                if (!parse_int(q, le, b)) {
+                    set_error("%s: malformed METIS header", path);
+                    return FC_ERR_FORMAT;
+                }
+                declared_nodes = a;
+                P.file_directed = (parse_int(q, le, c) && c == 100) ? 1 : 0;
+                header_done = true;
+                continue;
+            }
+            if (d10_line >= declared_nodes) continue;
+            while (parse_int(q, le, a)) {
+                if (a < 1 || !push(d10_line, a - 1)) {
+                    set_error("%s: malformed METIS adjacency", path);
+                    return FC_ERR_FORMAT;
+                }
+            }
+            ++d10_line;
+        }
+    }
+    if (fmt == 0) {
+        set_error("%s: empty file", path);
+        return FC_ERR_FORMAT;
+    }
+    long long nv = (relabel && fmt == 1) ? (long long)idmap.size() : declared_nodes;
+    if (nv < maxid + 1) nv = maxid + 1;
+    if (nv > INT_MAX) {
+        set_error("%s: %lld vertices exceed the int32 limit", path, nv);
+        return FC_ERR_OVERFLOW;
+    }
+    P.nv = nv;
+    return FC_OK;
+}
+
+struct CtxLock {
+    fc::DevCtx *c = nullptr;
+    int rc = FC_OK;
+    std::unique_lock<std::mutex> lk;
+    CtxLock()
+    {
+        c = fc::get_ctx(&rc);
+        if (c) lk = std::unique_lock<std::mutex>(c->mu);
+    }
+};
+
+cudaStream_t pick_stream(const fc_opts *o, fc::DevCtx *c)
+{
+    return (o && o->stream) ? (cudaStream_t)o->stream : c->stream;
+}
+
+fc_opts default_opts()
+{
+    fc_opts o;
+    fc_opts_init(&o);
+    return o;
+}
+
+}  // namespace
+
+extern "C" {
+
+void fc_opts_init(fc_opts *o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->sched = FC_SCHED_HEURISTIC;
+    o->engine = FC_ENGINE_AUTO;
+}
+
+int fc_version(void) { return 100; }
+
+const char *fc_strerror(int code)
+{
+    switch (code) {
+    case FC_OK: return "ok";
+    case FC_ERR_INVALID: return "invalid argument";
+    case FC_ERR_CUDA: return "CUDA error";
+    case FC_ERR_OOM: return "out of memory";
+    case FC_ERR_IO: return "I/O error";
+    case FC_ERR_FORMAT: return "malformed graph file";
+    case FC_ERR_TIMEOUT: return "device-side wait timed out";
+    case FC_ERR_OVERFLOW: return "graph exceeds int32 CSR limits";
+    case FC_ERR_NO_DEVICE: return "no CUDA device";
+    case FC_ERR_UNSUPPORTED: return "unsupported option";
+    default: return "unknown error";
+    }
+}
+
+int fc_device_info(int32_t *sm_count, int64_t *total_mem, int32_t *cc_major, int32_t *cc_minor)
+{
+    int dev = 0, n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return FC_ERR_NO_DEVICE;
+    cudaGetDevice(&dev);
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return FC_ERR_CUDA;
+    if (sm_count) *sm_count = p.multiProcessorCount;
+    if (total_mem) *total_mem = (int64_t)p.totalGlobalMem;
+    if (cc_major) *cc_major = p.major;
+    if (cc_minor) *cc_minor = p.minor;
+    return FC_OK;
+}
+
+int fc_graph_load_edgelist(const char *path, int force_dir, int relabel, fc_graph **g)
+{
+    if (validate_ptr(path, "path") || validate_ptr(g, "g")) return FC_ERR_INVALID;
+    *g = nullptr;
+    Parsed P;
+    int rc = parse_file(path, relabel, P);
+    if (rc) return rc;
+    int directed = force_dir == 0 ? 1 : force_dir == 1 ? 0 : (P.file_directed == 1 ? 1 : 0);
+    return fc_graph_from_edges(P.src.data(), P.dst.data(), (int64_t)P.src.size(), (int32_t)P.nv,
+                               directed ? FC_INGEST_DIRECTED : 0, g);
+}
+
+int fc_graph_from_csr(const int32_t *row_ptr, int32_t nv, const int32_t *col, int64_t ne,
+                      int directed, fc_graph **g)
+{
+    if (validate_ptr(row_ptr, "row_ptr") || validate_ptr(g, "g")) return FC_ERR_INVALID;
+    if (ne > 0 && validate_ptr(col, "col")) return FC_ERR_INVALID;
+    *g = nullptr;
+    if (nv <= 0 || ne < 0 || ne > INT_MAX) {
+        set_error("bad sizes nv=%d ne=%lld", nv, (long long)ne);
+        return FC_ERR_INVALID;
+    }
+    if (row_ptr[0] != 0 || (int64_t)row_ptr[nv] != ne) {
+        set_error("row_ptr must start at 0 and end at ne");
+        return FC_ERR_INVALID;
+    }
+    for (int32_t i = 0; i < nv; ++i)
+        if (row_ptr[i + 1] < row_ptr[i]) {
+            set_error("row_ptr decreases at %d", i);
+            return FC_ERR_INVALID;
+        }
+    for (int64_t j = 0; j < ne; ++j)
+        if (col[j] < 0 || col[j] >= nv) {
+            set_error("col[%lld] = %d out of range", (long long)j, col[j]);
+            return FC_ERR_INVALID;
+        }
+    CtxLock L;
+    if (!L.c) return L.rc;
+    cudaStream_t st = L.c->stream;
+    fc_graph *gg = new_graph(nv, directed ? 1 : 0);
+    if (!gg) return FC_ERR_OOM;
+    gg->ne = ne;
+    int rc = FC_OK;
+    if (cudaMalloc(&gg->row_ptr, sizeof(int32_t) * ((size_t)nv + 1)) != cudaSuccess ||
+        cudaMalloc(&gg->col, sizeof(int32_t) * (size_t)std::max<int64_t>(1, ne) + 16) != cudaSuccess) {
+        fc_graph_free(gg);
+        set_error("cudaMalloc failed for the CSR");
+        return FC_ERR_OOM;
+    }
+    if (cudaMemcpy(gg->row_ptr, row_ptr, sizeof(int32_t) * ((size_t)nv + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+        (ne > 0 && cudaMemcpy(gg->col, col, sizeof(int32_t) * (size_t)ne, cudaMemcpyHostToDevice) != cudaSuccess)) {
+        fc_graph_free(gg);
+        set_error("copy of the CSR failed");
+        return FC_ERR_CUDA;
+    }
+    rc = finish_graph(gg, st);
+    if (rc) {
+        fc_graph_free(gg);
+        return rc;
+    }
+    cudaStreamSynchronize(st);
+    *g = gg;
+    return FC_OK;
+}
+
+int fc_graph_from_edges(const int32_t *src, const int32_t *dst, int64_t n, int32_t nv, int flags,
+                        fc_graph **g)
+{
+    if (validate_ptr(g, "g")) return FC_ERR_INVALID;
+    if (n > 0 && (validate_ptr(src, "src") || validate_ptr(dst, "dst"))) return FC_ERR_INVALID;
+    *g = nullptr;
+    if (nv <= 0 || n < 0) {
+        set_error("bad sizes nv=%d n=%lld", nv, (long long)n);
+        return FC_ERR_INVALID;
+    }
+    CtxLock L;
+    if (!L.c) return L.rc;
+    cudaStream_t st = L.c->stream;
+    int32_t *ds = nullptr, *dd = nullptr;
+    size_t bytes = sizeof(int32_t) * (size_t)std::max<int64_t>(1, n);
+    if (cudaMalloc(&ds, bytes) != cudaSuccess || cudaMalloc(&dd, bytes) != cudaSuccess) {
+        cudaFree(ds);
+        set_error("cudaMalloc failed for the edge list");
+        return FC_ERR_OOM;
+    }
+    int rc = FC_OK;
+    if (n > 0 && (cudaMemcpyAsync(ds, src, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+                  cudaMemcpyAsync(dd, dst, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st) != cudaSuccess))
+        rc = FC_ERR_CUDA;
+    if (rc == FC_OK) rc = from_device_edges(ds, dd, n, nv, flags, g, st);
+    cudaStreamSynchronize(st);
+    cudaFree(ds);
+    cudaFree(dd);
+    return rc;
+}
+
+int fc_graph_from_device_edges(const int32_t *d_src, const int32_t *d_dst, int64_t n, int32_t nv,
+                               int flags, fc_graph **g)
+{
+    if (validate_ptr(g, "g")) return FC_ERR_INVALID;
+    *g = nullptr;
+    if (nv <= 0 || n < 0) return FC_ERR_INVALID;
+    CtxLock L;
+    if (!L.c) return L.rc;
+    int rc = from_device_edges(d_src, d_dst, n, nv, flags, g, L.c->stream);
+    cudaStreamSynchronize(L.c->stream);
+    return rc;
+}
+
+int fc_graph_generate_rmat(int32_t scale, int64_t nedges, double a, double b, double c,
+                           uint64_t seed, int64_t perm_seed, fc_graph **g)
+{
+    if (validate_ptr(g, "g")) return FC_ERR_INVALID;
+    *g = nullptr;
+    if (scale < 1 || scale > 30 || nedges < 0 || a < 0 || b < 0 || c < 0 || a + b + c > 1.0) {
+        set_error("bad R-MAT parameters");
+        return FC_ERR_INVALID;
+    }
+    CtxLock L;
+    if (!L.c) return L.rc;
+    cudaStream_t st = L.c->stream;
+    int32_t *ds = nullptr, *dd = nullptr;
+    size_t bytes = sizeof(int32_t) * (size_t)std::max<int64_t>(1, nedges);
+    if (cudaMalloc(&ds, bytes) != cudaSuccess || cudaMalloc(&dd, bytes) != cudaSuccess) {
+        cudaFree(ds);
+        set_error("cudaMalloc failed for the R-MAT edge list");
+        return FC_ERR_OOM;
+    }
+    int rc = fc::gen_rmat_device(scale, nedges, a, b, c, seed, perm_seed, ds, dd, st);
+    if (rc == FC_OK) rc = from_device_edges(ds, dd, nedges, 1 << scale, 0, g, st);
+    cudaStreamSynchronize(st);
+    cudaFree(ds);
+    cudaFree(dd);
+    return rc;
+}
+
+int fc_graph_generate_grid(int32_t w, int32_t h, double p_del, uint64_t del_seed, int64_t shortcuts,
+                           uint64_t sc_seed, fc_graph **g)
+{
+    if (validate_ptr(g, "g")) return FC_ERR_INVALID;
+    *g = nullptr;
+    if (w < 2 || h < 2 || (long long)w * h > INT_MAX || p_del < 0 || p_del > 1 || shortcuts < 0) {
+        set_error("bad grid parameters");
+        return FC_ERR_INVALID;
+    }
+    CtxLock L;
+    if (!L.c) return L.rc;
+    cudaStream_t st = L.c->stream;
+    long long slots = fc::grid_edge_slots(w, h, shortcuts);
+    int32_t *ds = nullptr, *dd = nullptr;
+    size_t bytes = sizeof(int32_t) * (size_t)std::max<long long>(1, slots);
+    if (cudaMalloc(&ds, bytes) != cudaSuccess || cudaMalloc(&dd, bytes) != cudaSuccess) {
+        cudaFree(ds);
+        set_error("cudaMalloc failed for the grid edge list");
+        return FC_ERR_OOM;
+    }
+    int rc = fc::gen_grid_device(w, h, p_del, del_seed, shortcuts, sc_seed, ds, dd, st);
+    if (rc == FC_OK) rc = from_device_edges(ds, dd, slots, w * h, 0, g, st);
+    cudaStreamSynchronize(st);
+    cudaFree(ds);
+    cudaFree(dd);
+    return rc;
+}
+
+int fc_graph_info(const fc_graph *g, int32_t *nv, int64_t *ne, int32_t *directed)
+{
+    if (validate_ptr(g, "g")) return FC_ERR_INVALID;
+    if (nv) *nv = g->nv;
+    if (ne) *ne = g->ne;
+    if (directed) *directed = g->directed;
+    return FC_OK;
+}
+
+int fc_graph_get_csr(const fc_graph *g, int32_t *row_ptr, int32_t *col)
+{
+    if (validate_ptr(g, "g")) return FC_ERR_INVALID;
+    if (row_ptr)
+        FC_CUDA_TRY(cudaMemcpy(row_ptr, g->row_ptr, sizeof(int32_t) * ((size_t)g->nv + 1),
+                               cudaMemcpyDeviceToHost));
+    if (col && g->ne > 0)
+        FC_CUDA_TRY(cudaMemcpy(col, g->col, sizeof(int32_t) * (size_t)g->ne, cudaMemcpyDeviceToHost));
+    return FC_OK;
+}
+
+void fc_graph_free(fc_graph *g)
+{
+    if (!g) return;
+    if (g->rrow_ptr && g->rrow_ptr != g->row_ptr) cudaFree(g->rrow_ptr);
+    if (g->rcol && g->rcol != g->col) cudaFree(g->rcol);
+    cudaFree(g->row_ptr);
+    cudaFree(g->col);
+    free(g);
+}
+
+int fc_bfs_levels_ex(fc_graph *g, int32_t s, int32_t *levels, const fc_opts *opts, fc_stats *stats)
+{
+    if (validate_ptr(g, "g")) return FC_ERR_INVALID;
+    if (s < 0 || s >= g->nv) {
+        set_error("source %d outside [0, %d)", s, g->nv);
+        return FC_ERR_INVALID;
+    }
+    fc_opts o = opts ? *opts : default_opts();
+    CtxLock L;
+    if (!L.c) return L.rc;
+    return fc::engine_bfs(L.c, pair_of(g), s, levels, o, stats, pick_stream(opts, L.c));
+}
+
+int fc_bfs_levels(fc_graph *g, int32_t s, int32_t *levels)
+{
+    if (validate_ptr(levels, "levels")) return FC_ERR_INVALID;
+    return fc_bfs_levels_ex(g, s, levels, nullptr, nullptr);
+}
+
+int fc_stcon_ex(fc_graph *g, int32_t s, int32_t t, int32_t *connected, int32_t *hops,
+                const fc_opts *opts, fc_stats *stats)
+{
+    if (validate_ptr(g, "g") || validate_ptr(connected, "connected") || validate_ptr(hops, "hops"))
+        return FC_ERR_INVALID;
+    if (s < 0 || s >= g->nv || t < 0 || t >= g->nv) {
+        set_error("query (%d, %d) outside [0, %d)", s, t, g->nv);
+        return FC_ERR_INVALID;
+    }
+    fc_opts o = opts ? *opts : default_opts();
+    CtxLock L;
+    if (!L.c) return L.rc;
+    return fc::engine_stcon(L.c, pair_of(g), s, t, connected, hops, o, stats, pick_stream(opts, L.c));
+}
+
+int fc_stcon(fc_graph *g, int32_t s, int32_t t, int32_t *connected, int32_t *hops)
+{
+    return fc_stcon_ex(g, s, t, connected, hops, nullptr, nullptr);
+}
+
+int fc_stcon_depth(fc_graph *g, int32_t s, int32_t t, int32_t *depth)
+{
+    if (validate_ptr(depth, "depth")) return FC_ERR_INVALID;
+    int32_t c = 0, h = -1;
+    int rc = fc_stcon(g, s, t, &c, &h);
+    if (rc) return rc;
+    *depth = c ? (h + 1) / 2 : -1;
+    return FC_OK;
+}
+
+int fc_stcon_batch_device(fc_graph *const *gs, int32_t ngraphs, const int32_t *d_graph_idx,
+                          const int32_t *d_s, const int32_t *d_t, int32_t nq, int32_t *d_connected,
+                          int32_t *d_hops, const fc_opts *opts, fc_stats *stats)
+{
+    if (validate_ptr(gs, "gs")) return FC_ERR_INVALID;
+    if (nq < 0 || ngraphs < 1) return FC_ERR_INVALID;
+    if (nq == 0) return FC_OK;
+    if (validate_ptr(d_s, "s") || validate_ptr(d_t, "t") || validate_ptr(d_connected, "connected") ||
+        validate_ptr(d_hops, "hops"))
+        return FC_ERR_INVALID;
+    std::vector<fc::GraphPairH> pairs((size_t)ngraphs);
+    for (int i = 0; i < ngraphs; ++i) {
+        if (!gs[i]) return FC_ERR_INVALID;
+        pairs[(size_t)i] = pair_of(gs[i]);
+    }
+    fc_opts o = opts ? *opts : default_opts();
+    CtxLock L;
+    if (!L.c) return L.rc;
+    return fc::engine_stcon_batch(L.c, pairs.data(), ngraphs, d_graph_idx, d_s, d_t, nq, d_connected,
+                                  d_hops, o, stats, pick_stream(opts, L.c), stats != nullptr);
+}
+
+int fc_stcon_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *graph_idx, const int32_t *s,
+                   const int32_t *t, int32_t nq, int32_t *connected, int32_t *hops,
+                   const fc_opts *opts, fc_stats *stats)
+{
+    if (validate_ptr(gs, "gs")) return FC_ERR_INVALID;
+    if (nq < 0 || ngraphs < 1) return FC_ERR_INVALID;
+    if (nq == 0) return FC_OK;
+    if (validate_ptr(s, "s") || validate_ptr(t, "t") || validate_ptr(connected, "connected") ||
+        validate_ptr(hops, "hops"))
+        return FC_ERR_INVALID;
+    for (int i = 0; i < ngraphs; ++i)
+        if (!gs[i]) return FC_ERR_INVALID;
+    for (int32_t i = 0; i < nq; ++i) {
+        int gi = graph_idx ? graph_idx[i] : 0;
+        if (gi < 0 || gi >= ngraphs) {
+            set_error("graph_idx[%d] = %d outside [0, %d)", i, gi, ngraphs);
+            return FC_ERR_INVALID;
+        }
+        if (s[i] < 0 || s[i] >= gs[gi]->nv || t[i] < 0 || t[i] >= gs[gi]->nv) {
+            set_error("query %d (%d, %d) outside [0, %d)", i, s[i], t[i], gs[gi]->nv);
+            return FC_ERR_INVALID;
+        }
+    }
+    CtxLock L;
+    if (!L.c) return L.rc;
+    cudaStream_t st = pick_stream(opts, L.c);
+    int32_t *buf = nullptr;
+    size_t k = (size_t)nq;
+    FC_CUDA_TRY(cudaMallocAsync(&buf, sizeof(int32_t) * k * 5, st));
+    int32_t *ds = buf, *dt = buf + k, *dg = buf + 2 * k, *dc = buf + 3 * k, *dh = buf + 4 * k;
+    FC_CUDA_TRY(cudaMemcpyAsync(ds, s, sizeof(int32_t) * k, cudaMemcpyHostToDevice, st));
+    FC_CUDA_TRY(cudaMemcpyAsync(dt, t, sizeof(int32_t) * k, cudaMemcpyHostToDevice, st));
+    if (graph_idx) FC_CUDA_TRY(cudaMemcpyAsync(dg, graph_idx, sizeof(int32_t) * k, cudaMemcpyHostToDevice, st));
+    std::vector<fc::GraphPairH> pairs((size_t)ngraphs);
+    for (int i = 0; i < ngraphs; ++i) pairs[(size_t)i] = pair_of(gs[i]);
+    fc_opts o = opts ? *opts : default_opts();
+    int rc = fc::engine_stcon_batch(L.c, pairs.data(), ngraphs, graph_idx ? dg : nullptr, ds, dt, nq,
+                                    dc, dh, o, stats, st, true);
+    if (rc == FC_OK) {
+        FC_CUDA_TRY(cudaMemcpyAsync(connected, dc, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, st));
+        FC_CUDA_TRY(cudaMemcpyAsync(hops, dh, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, st));
+        FC_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    cudaFreeAsync(buf, st);
+    cudaStreamSynchronize(st);
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,86 @@
+// fc_engine.h -- host-side interface of the traversal engines (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "fastcon.h"
+
+namespace fc {
+
+struct DGraphH {  // host copy of a device CSR
+    const int32_t *row_ptr;
+    const int32_t *col;
+    int32_t nv;
+    int32_t pad_;
+    int64_t ne;
+};
+
+// forward CSR (expands the s side) and reverse CSR (expands the t side);
+// identical for undirected graphs
+struct GraphPairH {
+    DGraphH fwd, rev;
+};
+
+struct TeamCounters;
+struct QueryStat {
+    long long inspected;
+    long long alg_bytes;
+    int steps;
+    int bu_steps;
+    int visited;
+    int escalated;
+};
+
+// Per-device context: workspaces grown on demand, events, the batched arena.
+struct DevCtx {
+    int device = -1;
+    int sm_count = 0;
+    int coop = 0;
+    std::mutex mu;
+    // persistent / host-loop workspace (one query at a time)
+    uint8_t *status = nullptr;
+    int32_t *levels = nullptr;
+    int32_t *log = nullptr;
+    size_t ws_nv = 0;
+    TeamCounters *tc = nullptr;      // device
+    TeamCounters *h_tc = nullptr;    // pinned mirror
+    void *d_graphs = nullptr;        // GraphPair table
+    size_t graphs_cap = 0;
+    // batched arena
+    uint8_t *b_status = nullptr;
+    int32_t *b_log = nullptr;
+    size_t b_slots = 0, b_status_stride = 0, b_log_stride = 0;
+    int b_log_cap = 0;
+    int *b_ctr = nullptr;            // [0] next query, [1] spill count, [2] error
+    int32_t *b_spill = nullptr;
+    size_t b_spill_cap = 0;
+    QueryStat *qstat = nullptr;
+    size_t qstat_cap = 0;
+    int32_t *d_tmp_q = nullptr;      // staging for host-array batches
+    size_t tmp_q_cap = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
+    cudaStream_t stream = nullptr;
+    // cached CUDA graph of the last batched launch
+    cudaGraphExec_t gexec = nullptr;
+    unsigned long long gkey = 0;
+};
+
+DevCtx *get_ctx(int *err);
+
+int engine_bfs(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_levels,
+               const fc_opts &o, fc_stats *st, cudaStream_t stream);
+
+int engine_stcon(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int32_t *conn,
+                 int32_t *hops, const fc_opts &o, fc_stats *st, cudaStream_t stream);
+
+int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int32_t *d_gi,
+                       const int32_t *d_s, const int32_t *d_t, int32_t nq, int32_t *d_conn,
+                       int32_t *d_hops, const fc_opts &o, fc_stats *st, cudaStream_t stream,
+                       bool sync);
+
+void set_error(const char *fmt, ...);
+
+}  // namespace fc

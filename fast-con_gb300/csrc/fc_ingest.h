@@ -1,0 +1,25 @@
+// fc_ingest.h -- device CSR construction and graph generators (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fc {
+
+// Build a canonical CSR from a device COO list (src[i] == -1 marks "no
+// edge").  On success *out_row_ptr / *out_col are new device allocations
+// owned by the caller.
+int ingest_device_edges(const int32_t *d_src, const int32_t *d_dst, long long n, int nv, int flags,
+                        int32_t **out_row_ptr, int32_t **out_col, long long *out_ne,
+                        cudaStream_t st);
+
+int gen_rmat_device(int scale, long long nedges, double a, double b, double c,
+                    unsigned long long seed, long long perm_seed, int32_t *d_src, int32_t *d_dst,
+                    cudaStream_t st);
+
+long long grid_edge_slots(int w, int h, long long shortcuts);
+
+int gen_grid_device(int w, int h, double p_del, unsigned long long del_seed, long long shortcuts,
+                    unsigned long long sc_seed, int32_t *d_src, int32_t *d_dst, cudaStream_t st);
+
+}  // namespace fc

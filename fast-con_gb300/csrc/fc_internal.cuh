@@ -1,0 +1,202 @@
+// fc_internal.cuh -- shared device/host definitions of the fastcon library.
+//
+// Layout of one graph in HBM (built by fc_ingest.cu):
+//   row_ptr  int32[nv + 1]   offsets, 256-byte aligned allocation
+//   col      int32[ne]       neighbours, rows sorted ascending, deduplicated
+//
+// Traversal state of one query slot:
+//   status   uint8[nv, padded to 16]   0xFF = unvisited, else side<<7 | min(level,127)
+//   log      int32[nv]                 every claimed vertex exactly once; side 0
+//                                      appends upward from log[0], side 1 downward
+//                                      from log[nv-1], so a side's frontier is always
+//                                      one contiguous range of the log
+// A full BFS (level-array output) uses int32 levels (-1 = unvisited) in place of
+// the status bytes and only side 0 of the log.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fastcon.h"
+
+#ifndef FC_BLOCK
+#define FC_BLOCK 256
+#endif
+
+namespace fc {
+
+constexpr uint8_t ST_UNVISITED = 0xFF;
+constexpr int LEVEL7_MAX = 126;  // bottom-up needs exact frontier codes: level+1 <= 126
+
+__host__ __device__ inline uint8_t st_code(int side, int level)
+{
+    return (uint8_t)((side << 7) | (level < 127 ? level : 127));
+}
+
+struct DGraph {
+    const int32_t *row_ptr;
+    const int32_t *col;
+    int32_t nv;
+    int32_t pad_;
+    int64_t ne;
+};
+
+// ---------------------------------------------------------------------------
+// warp helpers (hand-written PTX only for the special registers)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned lane_id()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ unsigned long long global_timer_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ int warp_inclusive_scan(int x)
+{
+    unsigned l = lane_id();
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (l >= (unsigned)o) x += y;
+    }
+    return x;
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+__device__ __forceinline__ int warp_sum_i(int x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// Loads that bypass L1: status, log and counters are written by other SMs
+// during the same kernel, and L1 is not coherent across SMs.
+__device__ __forceinline__ int ld_cg(const int *p) { return __ldcg(p); }
+__device__ __forceinline__ long long ld_cg(const long long *p) { return __ldcg(p); }
+__device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long *p)
+{
+    return __ldcg(p);
+}
+__device__ __forceinline__ uint8_t ld_cg_u8(const uint8_t *p)
+{
+    return (uint8_t)__ldcg((const unsigned char *)p);
+}
+
+__device__ __forceinline__ int ld_acquire_gpu(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Byte-granular claim on the status array: one 32-bit atomicCAS on the word
+// holding the byte.  Returns the byte value seen: ST_UNVISITED means this
+// thread claimed it.  The loop retries only when a neighbouring byte of the
+// same word changed in between; each byte changes at most once per step, so
+// it ends after at most four attempts.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint8_t claim_u8(uint8_t *status, int v, uint8_t code)
+{
+    unsigned *w = reinterpret_cast<unsigned *>(status + (v & ~3));
+    unsigned sh = (unsigned)(v & 3) * 8u;
+    unsigned old = __ldcg(w);
+#pragma unroll 1
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        uint8_t b = (uint8_t)((old >> sh) & 0xFFu);
+        if (b != ST_UNVISITED) return b;
+        unsigned nw = (old & ~(0xFFu << sh)) | ((unsigned)code << sh);
+        unsigned prev = atomicCAS(w, old, nw);
+        if (prev == old) return ST_UNVISITED;
+        old = prev;
+    }
+    return (uint8_t)((old >> sh) & 0xFFu);  // unreachable in practice
+}
+
+// ---------------------------------------------------------------------------
+// Software grid barrier for cooperative launches.  Every wait is bounded by
+// an iteration count and by %globaltimer; on expiry the barrier records
+// FC_ERR_TIMEOUT in *err and returns false, and the caller returns.
+// bar[0] = arrival count, bar[1] = generation.
+// ---------------------------------------------------------------------------
+constexpr unsigned long long BARRIER_TIMEOUT_NS = 2000000000ull;  // 2 s
+constexpr long long BARRIER_MAX_SPINS = 1ll << 25;
+
+__device__ __forceinline__ bool grid_barrier(int *bar, int *err, int nblocks)
+{
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        int gen = ld_acquire_gpu(bar + 1);
+        __threadfence();
+        int arrived = atomicAdd(bar, 1) + 1;
+        if (arrived == nblocks) {
+            atomicExch(bar, 0);
+            __threadfence();
+            st_release_gpu(bar + 1, gen + 1);
+        } else {
+            unsigned long long t0 = global_timer_ns();
+            long long spins = 0;
+            while (ld_acquire_gpu(bar + 1) == gen) {
+                if (++spins > BARRIER_MAX_SPINS ||
+                    ((spins & 255) == 0 && global_timer_ns() - t0 > BARRIER_TIMEOUT_NS)) {
+                    atomicCAS(err, 0, FC_ERR_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        if (ok && ld_acquire_gpu(err) != 0) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+}  // namespace fc
+
+// ---------------------------------------------------------------------------
+// host-side helpers
+// ---------------------------------------------------------------------------
+#define FC_CUDA_TRY(expr)                                   \
+    do {                                                    \
+        cudaError_t e_ = (expr);                            \
+        if (e_ != cudaSuccess) {                            \
+            fc_set_last_cuda_error(e_, #expr, __FILE__, __LINE__); \
+            return e_ == cudaErrorMemoryAllocation ? FC_ERR_OOM : FC_ERR_CUDA; \
+        }                                                   \
+    } while (0)
+
+extern "C" void fc_set_last_cuda_error(cudaError_t e, const char *what, const char *file, int line);
+
+namespace fc {
+void set_error(const char *fmt, ...);  // thread-local message for fc_last_error_message
+}

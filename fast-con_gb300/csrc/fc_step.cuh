@@ -1,0 +1,314 @@
+// fc_step.cuh -- one expansion step of one side, for any team of CTAs.
+//
+// A "team" is the set of CTAs that cooperates on one query: the whole
+// cooperative grid (persistent engine), every CTA of an ordinary launch
+// (host-loop engine), or a single CTA (batched engine).  The step functions
+// take the team rank/size and never synchronise across CTAs themselves; the
+// engine puts a team barrier between steps.
+//
+// Top-down expansion balances load by degree class (after Merrill, Garland &
+// Grimshaw, "Scalable GPU Graph Traversal", PPoPP 2012):
+//   rows >= BLOCK entries   -> the whole CTA walks the row
+//   rows >= 32 entries      -> one warp walks the row
+//   smaller rows            -> CTA prefix scan of the degrees, the row offsets are
+//                              staged in shared memory and gathered by all threads
+// Rows are walked with 16-byte int4 loads of the column array (scalar loads only
+// for the unaligned head and tail).  Newly claimed vertices are appended to the
+// log with a warp ballot/shuffle scan and one atomicAdd per warp.
+#pragma once
+
+#include "fc_internal.cuh"
+
+namespace fc {
+
+constexpr int GATHER_PER_THREAD = 4;
+
+struct AppendTarget {
+    int32_t *log;       // log base of the slot
+    int32_t nv;         // graph size: side 1 writes log[nv - 1 - pos]
+    int32_t side;
+    int *tail;          // cumulative append counter of this side
+    unsigned long long *deg;  // cumulative degree sum of appended vertices
+    const int32_t *row_ptr;   // CSR used to expand this side next time
+};
+
+__device__ __forceinline__ void log_write(const AppendTarget &a, int pos, int v)
+{
+    if (a.side == 0)
+        a.log[pos] = v;
+    else
+        a.log[a.nv - 1 - pos] = v;
+}
+
+// All 32 lanes of the warp must call this with the same K.
+template <int K>
+__device__ __forceinline__ void warp_append(const int (&c)[K], const AppendTarget &a)
+{
+    int cnt = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) cnt += c[k] >= 0;
+    unsigned any = __ballot_sync(0xffffffffu, cnt > 0);
+    if (!any) return;
+    int incl = warp_inclusive_scan(cnt);
+    int total = __shfl_sync(0xffffffffu, incl, 31);
+    long long dsum = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        if (c[k] >= 0) dsum += __ldg(a.row_ptr + c[k] + 1) - __ldg(a.row_ptr + c[k]);
+    dsum = warp_sum_ll(dsum);
+    int base = 0;
+    if (lane_id() == 0) {
+        base = atomicAdd(a.tail, total);
+        atomicAdd(a.deg, (unsigned long long)dsum);
+    }
+    base = __shfl_sync(0xffffffffu, base, 0);
+    int pos = base + incl - cnt;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        if (c[k] >= 0) log_write(a, pos++, c[k]);
+}
+
+// ---------------------------------------------------------------------------
+// Visitors: what happens at one neighbour v of a frontier vertex.
+// visit() returns v when this thread claimed it, else -1.
+// ---------------------------------------------------------------------------
+struct VisitSTCON {
+    uint8_t *status;
+    uint8_t next_code;  // st_code(side, level + 1)
+    int side;
+    int *found;
+    __device__ __forceinline__ int visit(int v) const
+    {
+        uint8_t s = ld_cg_u8(status + v);
+        if (s == ST_UNVISITED) {
+            s = claim_u8(status, v, next_code);
+            if (s == ST_UNVISITED) return v;
+        }
+        if ((int)(s >> 7) != side) *(volatile int *)found = 1;
+        return -1;
+    }
+};
+
+struct VisitBFS {
+    int32_t *levels;
+    int32_t next_level;
+    __device__ __forceinline__ int visit(int v) const
+    {
+        if (ld_cg(levels + v) >= 0) return -1;
+        return atomicCAS(levels + v, -1, next_level) == -1 ? v : -1;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Walk col[b, e) with `nlanes` threads (lane_idx in [0, nlanes)); every warp
+// of the group must call it (loop trip counts are uniform per warp).
+// ---------------------------------------------------------------------------
+template <class Vis>
+__device__ __forceinline__ void walk_range(const int32_t *__restrict__ col, int b, int e,
+                                           int lane_idx, int nlanes, const Vis &vis,
+                                           const AppendTarget &app)
+{
+    int a = min((b + 3) & ~3, e);
+    int z = max(e & ~3, a);
+    int nhead = a - b, ntail = e - z;
+    if (nhead + ntail > 0 && lane_idx < 32) {
+        // at most 6 scalar entries: only the group's first warp takes part
+        int c[1] = {-1};
+        if (lane_idx < nhead)
+            c[0] = vis.visit(__ldg(col + b + lane_idx));
+        else if (lane_idx < nhead + ntail)
+            c[0] = vis.visit(__ldg(col + z + lane_idx - nhead));
+        warp_append<1>(c, app);
+    }
+    const int4 *col4 = reinterpret_cast<const int4 *>(col);
+    const int k_end = z >> 2;
+    for (int k0 = a >> 2; k0 < k_end; k0 += nlanes) {
+        int k = k0 + lane_idx;
+        int c[4] = {-1, -1, -1, -1};
+        if (k < k_end) {
+            int4 x = __ldg(col4 + k);
+            c[0] = vis.visit(x.x);
+            c[1] = vis.visit(x.y);
+            c[2] = vis.visit(x.z);
+            c[3] = vis.visit(x.w);
+        }
+        warp_append<4>(c, app);
+    }
+}
+
+template <int T>
+struct SmemTopDown {
+    int owner;
+    int rb, re;
+    int stop;
+    int warp_tot[T / 32];
+    int total;
+    int gather[T * GATHER_PER_THREAD];
+};
+
+// Block-wide inclusive scan of x; *total receives the sum.  All threads call.
+template <int T>
+__device__ __forceinline__ int block_inclusive_scan(int x, int *warp_tot, int *total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = warp_inclusive_scan(x);
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        int w = lane < T / 32 ? warp_tot[lane] : 0;
+        int wi = warp_inclusive_scan(w);
+        if (lane < T / 32) warp_tot[lane] = wi - w;  // exclusive prefix of warps
+        if (lane == 31) *total = wi;
+    }
+    __syncthreads();
+    int r = incl + warp_tot[wid];
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Top-down step over frontier[0, F).  Tiles of T frontier vertices are dealt
+// round-robin to the team's CTAs.  `stop_flag` (nullable) is polled once per
+// tile; a set flag ends the step early (used when the two sides have met).
+// ---------------------------------------------------------------------------
+template <int T, class Vis>
+__device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
+                             const int32_t *frontier, int F, int team_rank, int team_size,
+                             const Vis &vis, const AppendTarget &app, SmemTopDown<T> &sm,
+                             const int *stop_flag)
+{
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (long long base = (long long)team_rank * T; base < F; base += (long long)team_size * T) {
+        int i = (int)base + tid;
+        int rb = 0, re = 0;
+        if (i < F) {
+            int u = ld_cg(frontier + i);
+            rb = __ldg(row_ptr + u);
+            re = __ldg(row_ptr + u + 1);
+        }
+        // class 1: rows of >= T entries, whole CTA
+        while (true) {
+            if (tid == 0) sm.owner = -1;
+            __syncthreads();
+            if (re - rb >= T) sm.owner = tid;
+            __syncthreads();
+            int w = sm.owner;
+            if (w < 0) break;
+            if (tid == w) {
+                sm.rb = rb;
+                sm.re = re;
+                rb = re;
+            }
+            __syncthreads();
+            walk_range(col, sm.rb, sm.re, tid, T, vis, app);
+        }
+        // class 2: rows of >= 32 entries, one warp
+        while (true) {
+            unsigned m = __ballot_sync(0xffffffffu, re - rb >= 32);
+            if (!m) break;
+            int leader = __ffs(m) - 1;
+            int b = __shfl_sync(0xffffffffu, rb, leader);
+            int e = __shfl_sync(0xffffffffu, re, leader);
+            if (lane == leader) rb = re;
+            walk_range(col, b, e, lane, 32, vis, app);
+        }
+        // class 3: short rows, CTA scan + shared-memory gather
+        int d = re - rb;
+        int incl = block_inclusive_scan<T>(d, sm.warp_tot, &sm.total);
+        int off = incl - d;
+        const int total = sm.total;
+        constexpr int G = T * GATHER_PER_THREAD;
+        for (int chunk = 0; chunk < total; chunk += G) {
+            int lo = max(off, chunk), hi = min(off + d, chunk + G);
+            for (int j = lo; j < hi; ++j) sm.gather[j - chunk] = rb + (j - off);
+            __syncthreads();
+            int cnt = min(G, total - chunk);
+            for (int k0 = 0; k0 < cnt; k0 += T) {
+                int k = k0 + tid;
+                int c[1] = {-1};
+                if (k < cnt) c[0] = vis.visit(__ldg(col + sm.gather[k]));
+                warp_append<1>(c, app);
+            }
+            __syncthreads();
+        }
+        if (stop_flag) {
+            if (tid == 0) sm.stop = *(volatile const int *)stop_flag;
+            __syncthreads();
+            if (sm.stop) break;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Bottom-up step.  Every vertex v of [0, nv) not yet owned by the expanding
+// side scans its (reverse-graph) neighbours for one in the expanding side's
+// frontier and stops at the first hit:
+//   v unvisited                 -> v joins the side at level + 1
+//   v owned by the other side,
+//   at that side's frontier     -> meeting
+// Only the thread that owns v writes v's status, so no CAS is needed, and the
+// new code (level + 1) never equals the frontier code (level): no chaining.
+// ---------------------------------------------------------------------------
+struct BottomUpSTCON {
+    uint8_t *status;
+    uint8_t front_code;   // st_code(side, level)
+    uint8_t next_code;    // st_code(side, level + 1)
+    uint8_t other_front;  // st_code(other side, its radius)
+    int *found;
+    __device__ __forceinline__ int check(int v, const int32_t *__restrict__ row_ptr,
+                                         const int32_t *__restrict__ col, int &inspected) const
+    {
+        uint8_t s = ld_cg_u8(status + v);
+        bool unvisited = s == ST_UNVISITED;
+        if (!unvisited && s != other_front) return -1;
+        int b = __ldg(row_ptr + v), e = __ldg(row_ptr + v + 1);
+        for (int j = b; j < e; ++j) {
+            ++inspected;
+            if (ld_cg_u8(status + __ldg(col + j)) == front_code) {
+                if (unvisited) {
+                    status[v] = next_code;
+                    return v;
+                }
+                *(volatile int *)found = 1;
+                return -1;
+            }
+        }
+        return -1;
+    }
+};
+
+struct BottomUpBFS {
+    int32_t *levels;
+    int32_t level;  // frontier level
+    __device__ __forceinline__ int check(int v, const int32_t *__restrict__ row_ptr,
+                                         const int32_t *__restrict__ col, int &inspected) const
+    {
+        if (ld_cg(levels + v) >= 0) return -1;
+        int b = __ldg(row_ptr + v), e = __ldg(row_ptr + v + 1);
+        for (int j = b; j < e; ++j) {
+            ++inspected;
+            if (ld_cg(levels + __ldg(col + j)) == level) {
+                levels[v] = level + 1;
+                return v;
+            }
+        }
+        return -1;
+    }
+};
+
+template <int T, class BU>
+__device__ void bottomup_step(const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
+                              int nv, int team_rank, int team_size, const BU &bu,
+                              const AppendTarget &app, unsigned long long *inspected_total)
+{
+    int inspected = 0;
+    for (long long v0 = (long long)team_rank * T; v0 < nv; v0 += (long long)team_size * T) {
+        int v = (int)v0 + threadIdx.x;
+        int c[1] = {-1};
+        if (v < nv) c[0] = bu.check(v, row_ptr, col, inspected);
+        warp_append<1>(c, app);
+    }
+    int w = warp_sum_i(inspected);
+    if (lane_id() == 0 && w) atomicAdd(inspected_total, (unsigned long long)w);
+}
+
+}  // namespace fc

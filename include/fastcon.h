@@ -1,0 +1,189 @@
+/*
+ * fastcon.h -- C ABI of the GB300-native ST-CON / BFS library (libfastcon.so).
+ *
+ * Plain C: opaque handles, int32/int64 arrays, int status codes; no C++ or
+ * torch types cross this boundary and nothing aborts the process.  A graph
+ * handle owns all device memory it uses; calls on one handle must be
+ * serialised by the caller (one handle per host thread, or a lock).
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the reference project root; S/ = bernaschi/ST_CONN_ONE_ATOMIC/current-st/
+ * st-conn/, K/ = BFS-4K/).
+ *
+ * Answer semantics (all integer, bit-exact against the reference CPU path
+ * Graph::bfs, K/src/host/graph.cpp:83-97):
+ *   levels[v]  = hop distance from s, -1 where the reference stores INF
+ *   connected  = (levels[t] != -1), hops = levels[t] (-1 when not connected)
+ */
+#ifndef FASTCON_H
+#define FASTCON_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define FC_OK              0
+#define FC_ERR_INVALID     1  /* bad argument: null pointer, vertex out of range, bad CSR */
+#define FC_ERR_CUDA        2  /* a CUDA call failed (fc_last_error_message has details)   */
+#define FC_ERR_OOM         3  /* device or host allocation failed                         */
+#define FC_ERR_IO          4  /* file cannot be opened / read                             */
+#define FC_ERR_FORMAT      5  /* file contents cannot be parsed                           */
+#define FC_ERR_TIMEOUT     6  /* a bounded device-side wait expired (kernel returned)     */
+#define FC_ERR_OVERFLOW    7  /* graph exceeds the int32 CSR limits                        */
+#define FC_ERR_NO_DEVICE   8  /* no CUDA device                                            */
+#define FC_ERR_UNSUPPORTED 9  /* option combination not supported                          */
+
+/* ---- ingest flags (fc_graph_from_edges*) -------------------------------- */
+#define FC_INGEST_DIRECTED   1  /* keep (u,v) only; default adds (v,u) for every edge   */
+#define FC_INGEST_KEEP_LOOPS 2  /* keep self-loops; default drops them                  */
+#define FC_INGEST_KEEP_DUPS  4  /* keep repeated edges; default keeps one copy          */
+
+/* ---- scheduling policies ----------------------------------------------- */
+#define FC_SCHED_PLAIN     0  /* alternate s-side and t-side, top-down only            */
+#define FC_SCHED_HEURISTIC 1  /* side with the smaller frontier-edge sum first;
+                                 bottom-up when the frontier's edges exceed the
+                                 unexplored edges / 14 (fixed thresholds)               */
+#define FC_SCHED_LEARNED   2  /* MLP chooses side x direction x variant; uses the
+                                 heuristic until weights are loaded                    */
+
+/* ---- execution engines ------------------------------------------------- */
+#define FC_ENGINE_AUTO       0
+#define FC_ENGINE_HOSTLOOP   1  /* one kernel launch per level, host reads counters   */
+#define FC_ENGINE_PERSISTENT 2  /* one cooperative launch, grid barrier per level     */
+#define FC_ENGINE_BATCHED    3  /* many queries per launch, one CTA per query         */
+
+typedef struct fc_graph fc_graph;
+
+typedef struct fc_opts {
+    int32_t sched;        /* FC_SCHED_*                                     */
+    int32_t engine;       /* FC_ENGINE_*                                    */
+    int32_t block;        /* threads per CTA: 128, 256 or 512 (0 = tuned)   */
+    int32_t ctas_per_sm;  /* resident CTAs per SM for batched (0 = tuned)   */
+    int32_t use_graph;    /* batched: capture the launch in a CUDA graph    */
+    int32_t max_slots;    /* batched: cap on concurrent queries (0 = all)   */
+    void   *stream;       /* cudaStream_t, NULL = the handle's own stream   */
+    int32_t reserved[8];
+} fc_opts;
+
+typedef struct fc_stats {
+    int64_t edges_inspected;  /* adjacency entries read by expansion steps   */
+    int64_t visited;          /* vertices claimed                            */
+    int32_t steps;            /* expansion steps (levels of either side)     */
+    int32_t bottom_up_steps;
+    double  gpu_ms;           /* device time of the call (CUDA events)       */
+    int64_t alg_bytes;        /* algorithmic HBM bytes of all steps: 4-byte
+                                 status words, 8 per row range, 4 per column
+                                 and queue entry (top-down 12|F| + 8E_F + 8|N|;
+                                 bottom-up 12 per scanned vertex + 8 per
+                                 neighbour checked + 8|N|)                    */
+    int32_t escalated;        /* batched: queries finished by the grid engine */
+    int32_t launches;         /* kernels launched by the call                 */
+    double  kernel_ms[2];     /* batched: [0] CTA-per-query kernel,
+                                 [1] grid kernel for escalated queries       */
+    int64_t kernel_alg_bytes[2]; /* alg_bytes of the queries each kernel
+                                    finished (same split as kernel_ms)       */
+} fc_stats;
+
+void fc_opts_init(fc_opts *o);
+
+/* ---- graphs ------------------------------------------------------------ */
+
+/* Load an edge-list file and build the CSR on the device.  Replaces
+ * load_graph (S/load_graph.c:20-104; SNAP "# Nodes: N Edges: M" header, raw
+ * ids) followed by run_make_struct (S/make_struct.c:39), and
+ * readGraph::readGraphHeader + readSTD (K/Util/readGraph.h:18-20; SNAP,
+ * MatrixMarket, DIMACS9, DIMACS10 detected from the first token).
+ * force_dir: -1 = as the file says (undirected when unspecified, as the
+ * bernaschi driver forces), 0 = directed, 1 = undirected.  relabel != 0
+ * renumbers SNAP ids by first appearance (BFS-4K), 0 keeps raw ids. */
+int fc_graph_load_edgelist(const char *path, int force_dir, int relabel, fc_graph **g);
+
+/* Adopt a finished CSR from host memory (copied into 128-byte-aligned device
+ * arrays).  Replaces Graph::ToCSR's output handed to
+ * cudaGraph::cudaGraph(Graph&) (K/include/device/cudaGraph.cuh:14-35).
+ * row_ptr must be non-decreasing with row_ptr[0] = 0, row_ptr[nv] = ne, and
+ * every col entry in [0, nv).  directed = 0 promises the CSR is symmetric. */
+int fc_graph_from_csr(const int32_t *row_ptr, int32_t nv, const int32_t *col, int64_t ne,
+                      int directed, fc_graph **g);
+
+/* Build the CSR on the device from a host COO edge list.  Replaces
+ * make_g_undirect + make_own_csr_nomulti (S/make_struct.c:304-359,
+ * 553-738): symmetrise, drop self-loops, sort, deduplicate (see FC_INGEST_*). */
+int fc_graph_from_edges(const int32_t *src, const int32_t *dst, int64_t n, int32_t nv,
+                        int flags, fc_graph **g);
+
+/* Same, with the edge list already in device memory (left untouched). */
+int fc_graph_from_device_edges(const int32_t *d_src, const int32_t *d_dst, int64_t n,
+                               int32_t nv, int flags, fc_graph **g);
+
+/* Seeded synthetic graphs generated and ingested on the device (no host
+ * copy of the edge list).  The generators follow fastcon/graphs.py bit for
+ * bit.  The R-MAT generator stands in for the reference's Graph500 driver
+ * path make_graph -> run_make_struct (S/main.c:358-371): nedges samples
+ * with initiator (a, b, c, 1-a-b-c), vertex ids permuted by a seeded
+ * bijection when perm_seed >= 0. */
+int fc_graph_generate_rmat(int32_t scale, int64_t nedges, double a, double b, double c,
+                           uint64_t seed, int64_t perm_seed, fc_graph **g);
+/* w x h 4-neighbour grid, each edge dropped with probability p_del, plus
+ * `shortcuts` uniformly random extra edges. */
+int fc_graph_generate_grid(int32_t w, int32_t h, double p_del, uint64_t del_seed,
+                           int64_t shortcuts, uint64_t sc_seed, fc_graph **g);
+
+int fc_graph_info(const fc_graph *g, int32_t *nv, int64_t *ne, int32_t *directed);
+/* Copy the device CSR back (row_ptr: nv+1 entries, col: ne entries). */
+int fc_graph_get_csr(const fc_graph *g, int32_t *row_ptr, int32_t *col);
+void fc_graph_free(fc_graph *g);
+
+/* ---- queries ------------------------------------------------------------ */
+
+/* Full BFS level array from s (host output, nv entries, -1 = unreachable).
+ * Replaces cudaGraph::Reset + cudaBFS4K (K/src/device/BFS_WorkEfficient.cu:
+ * 81-133) whose result is left in devDistance, and Graph::BfsInit + bfs on
+ * the host (K/src/host/graph.cpp:70-97). */
+int fc_bfs_levels(fc_graph *g, int32_t s, int32_t *levels);
+int fc_bfs_levels_ex(fc_graph *g, int32_t s, int32_t *levels, const fc_opts *opts,
+                     fc_stats *stats);
+
+/* One s-t connectivity query: connected flag and exact hop distance (-1 when
+ * not connected).  Replaces make_stcon (S/include/make_stcon.h:11-17,
+ * S/make_stcon.c:730-1497), which returns only DEPTH = ceil(d/2), and the
+ * double-source BFS of BFS_4K_DS (BFS_4K_DS/src/device/BFS_WorkEfficient.cu:
+ * 110-162), which returns only found / not found. */
+int fc_stcon(fc_graph *g, int32_t s, int32_t t, int32_t *connected, int32_t *hops);
+int fc_stcon_ex(fc_graph *g, int32_t s, int32_t t, int32_t *connected, int32_t *hops,
+                const fc_opts *opts, fc_stats *stats);
+
+/* Compatibility shim for make_stcon's return value: depth = ceil(hops / 2)
+ * (simultaneous two-sided rounds), -1 when not connected, 0 when s == t. */
+int fc_stcon_depth(fc_graph *g, int32_t s, int32_t t, int32_t *depth);
+
+/* Many queries, possibly over several graphs, in one call (host arrays).
+ * graph_idx[i] selects gs[graph_idx[i]] (graph_idx may be NULL: all on
+ * gs[0]).  Replaces the per-query loop of run_make_stcon
+ * (S/make_stcon.c:416-576) and the one-CTA-per-source launch of
+ * BFS_4K_BLOCK (BFS_4K_BLOCK/src/device/BFS_WorkEfficient.cu:64-206). */
+int fc_stcon_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *graph_idx,
+                   const int32_t *s, const int32_t *t, int32_t nq, int32_t *connected,
+                   int32_t *hops, const fc_opts *opts, fc_stats *stats);
+
+/* Same with every array in device memory (inputs resident in HBM); the
+ * call is asynchronous on the chosen stream unless stats is non-NULL. */
+int fc_stcon_batch_device(fc_graph *const *gs, int32_t ngraphs, const int32_t *d_graph_idx,
+                          const int32_t *d_s, const int32_t *d_t, int32_t nq,
+                          int32_t *d_connected, int32_t *d_hops, const fc_opts *opts,
+                          fc_stats *stats);
+
+/* ---- misc ---------------------------------------------------------------- */
+const char *fc_strerror(int code);
+const char *fc_last_error_message(void);  /* thread-local detail of the last error */
+int fc_device_info(int32_t *sm_count, int64_t *total_mem, int32_t *cc_major,
+                   int32_t *cc_minor);
+int fc_version(void);  /* major*10000 + minor*100 + patch */
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FASTCON_H */

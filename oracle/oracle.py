@@ -1,0 +1,185 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so) and of the
+reference's own CPU BFS compiled into oracle/_ref/libref_bfs.so.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
+by bench.py's CPU-baseline leg, always as the checker.  The product library
+never loads it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_BFS_PATH = os.path.join(HERE, "_ref", "libref_bfs.so")
+REF_GEN_PATH = os.path.join(HERE, "_ref", "graph500_gen")
+
+SYMMETRIZE, DROP_LOOPS, DEDUPE = 1, 2, 4
+CANONICAL = SYMMETRIZE | DROP_LOOPS | DEDUPE
+
+_lib = None
+_ref = None
+
+
+def build(ref_root: str | None = None) -> None:
+    """Compile liboracle.so; also oracle/_ref when the reference sources are
+    present at ref_root."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    if ref_root and os.path.isdir(ref_root):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
+
+
+def _P(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.oracle_bfs_levels.restype = ctypes.c_int32
+        L.oracle_bfs_levels.argtypes = [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p]
+        for fn in (L.oracle_stcon_batch, L.oracle_stcon_bidir_batch):
+            fn.restype = ctypes.c_int
+            fn.argtypes = [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                           ctypes.c_void_p, ctypes.c_int]
+        L.oracle_build_csr.restype = ctypes.c_int64
+        L.oracle_build_csr.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_void_p]
+        L.oracle_build_csr_mt.restype = ctypes.c_int64
+        L.oracle_build_csr_mt.argtypes = [ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_int]
+        L.oracle_gen_rmat.restype = None
+        L.oracle_gen_rmat.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                      ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_int]
+        L.oracle_count_visited_edges.restype = ctypes.c_int64
+        L.oracle_count_visited_edges.argtypes = [ctypes.c_int32, ctypes.c_void_p,
+                                                 ctypes.c_void_p, ctypes.c_void_p]
+        L.oracle_read_edgelist.restype = ctypes.c_int
+        L.oracle_read_edgelist.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def bfs_levels(row_ptr, col, src):
+    """Levels from src (-1 unreachable) and edges inspected."""
+    row_ptr, col = _i32(row_ptr), _i32(col)
+    nv = len(row_ptr) - 1
+    lev = np.empty(nv, np.int32)
+    q = np.empty(nv, np.int32)
+    ins = np.zeros(1, np.int64)
+    lib().oracle_bfs_levels(nv, _P(row_ptr), _P(col), int(src), _P(lev), _P(q), _P(ins))
+    return lev, int(ins[0])
+
+
+def stcon_batch(row_ptr, col, s, t, nthreads=1, bidir=False):
+    """(connected int32[nq], hops int32[nq], edges_inspected int64[nq])."""
+    row_ptr, col, s, t = _i32(row_ptr), _i32(col), _i32(s), _i32(t)
+    nv = len(row_ptr) - 1
+    nq = len(s)
+    conn = np.zeros(nq, np.int32)
+    hops = np.zeros(nq, np.int32)
+    ins = np.zeros(nq, np.int64)
+    fn = lib().oracle_stcon_bidir_batch if bidir else lib().oracle_stcon_batch
+    rc = fn(nv, _P(row_ptr), _P(col), nq, _P(s), _P(t), _P(conn), _P(hops), _P(ins),
+            int(nthreads))
+    if rc != 0:
+        raise ValueError("oracle_stcon_batch: vertex id out of range")
+    return conn, hops, ins
+
+
+def build_csr(nv, src, dst, flags=CANONICAL, nthreads=1):
+    src, dst = _i32(src), _i32(dst)
+    rp = np.zeros(nv + 1, np.int32)
+    cap = 2 * len(src) if flags & SYMMETRIZE else len(src)
+    col = np.zeros(max(1, cap), np.int32)
+    ne = lib().oracle_build_csr_mt(int(nv), len(src), _P(src), _P(dst), int(flags), _P(rp),
+                                   _P(col), int(nthreads))
+    if ne < 0:
+        raise ValueError("oracle_build_csr: bad edge list")
+    return rp, (col[:ne].copy() if ne < len(col) // 2 else col[:ne])
+
+
+def gen_rmat(scale, nedges, a=0.57, b=0.19, c=0.19, seed=3, perm_seed=-1, nthreads=1):
+    """R-MAT samples (same hash stream as fastcon/graphs.py and the GPU)."""
+    src = np.empty(max(1, nedges), np.int32)
+    dst = np.empty(max(1, nedges), np.int32)
+    lib().oracle_gen_rmat(int(scale), int(nedges), float(a), float(b), float(c), int(seed),
+                          int(perm_seed), _P(src), _P(dst), int(nthreads))
+    return src[:nedges], dst[:nedges]
+
+
+def count_visited_edges(row_ptr, col, levels):
+    row_ptr, col, levels = _i32(row_ptr), _i32(col), _i32(levels)
+    return int(lib().oracle_count_visited_edges(len(row_ptr) - 1, _P(row_ptr), _P(col),
+                                                _P(levels)))
+
+
+def read_edgelist(path, relabel=False):
+    """(nv, src int32, dst int32, file_directed)."""
+    nv = np.zeros(1, np.int32)
+    n = np.zeros(1, np.int64)
+    fd = np.zeros(1, np.int32)
+    rc = lib().oracle_read_edgelist(path.encode(), int(relabel), _P(nv), _P(n), _P(fd), None, None)
+    if rc != 0:
+        raise ValueError(f"oracle_read_edgelist: cannot parse {path}")
+    src = np.zeros(max(1, int(n[0])), np.int32)
+    dst = np.zeros(max(1, int(n[0])), np.int32)
+    rc = lib().oracle_read_edgelist(path.encode(), int(relabel), _P(nv), _P(n), _P(fd),
+                                    _P(src), _P(dst))
+    if rc != 0:
+        raise ValueError(f"oracle_read_edgelist: cannot parse {path}")
+    return int(nv[0]), src[: int(n[0])], dst[: int(n[0])], int(fd[0])
+
+
+# ---------------------------------------------------------------------------
+# The reference's own CPU BFS (compiled from its sources; present only where
+# the reference tree was available at build time).
+# ---------------------------------------------------------------------------
+def ref_available() -> bool:
+    return os.path.exists(REF_BFS_PATH)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        R = ctypes.CDLL(REF_BFS_PATH)
+        R.ref_bfs_many.restype = ctypes.c_int
+        R.ref_bfs_many.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p]
+        R.ref_inf.restype = ctypes.c_int
+        _ref = R
+    return _ref
+
+
+def ref_bfs_levels(row_ptr, col, sources):
+    """Reference Graph::bfs distances, INF mapped to -1: int32[len(sources), nv]."""
+    row_ptr, col = _i32(row_ptr), _i32(col)
+    src = _i32(sources)
+    nv = len(row_ptr) - 1
+    dist = np.zeros((len(src), nv), np.int32)
+    vis = np.zeros(len(src), np.int32)
+    ref().ref_bfs_many(nv, len(col), _P(row_ptr), _P(col), len(src), _P(src), _P(dist), _P(vis))
+    inf = ref().ref_inf()
+    dist[dist == inf] = -1
+    return dist, vis

@@ -1,0 +1,299 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+reference's golden outputs.  All answers are integers and must match exactly.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+from conftest import known_answer_graph
+
+from fastcon import graphs
+
+pytestmark = pytest.mark.gpu
+
+ENGINES_SINGLE = ["hostloop", "persistent"]
+ENGINES_BATCH = ["batched", "persistent", "hostloop"]
+SCHEDS = ["plain", "heuristic", "learned"]
+
+
+def sha_levels(lev):
+    return hashlib.sha256(np.ascontiguousarray(lev, dtype="<i4").tobytes()).hexdigest()
+
+
+def sha_csr(rp, col):
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(rp, dtype="<i4").tobytes())
+    h.update(np.ascontiguousarray(col, dtype="<i4").tobytes())
+    return h.hexdigest()
+
+
+def opts(fc, engine="persistent", sched="heuristic"):
+    e = {"auto": fc.ENGINE_AUTO, "hostloop": fc.ENGINE_HOSTLOOP,
+         "persistent": fc.ENGINE_PERSISTENT, "batched": fc.ENGINE_BATCHED}[engine]
+    s = {"plain": fc.SCHED_PLAIN, "heuristic": fc.SCHED_HEURISTIC,
+         "learned": fc.SCHED_LEARNED}[sched]
+    return fc.make_opts(sched=s, engine=e)
+
+
+# --------------------------------------------------------------------------
+# tiny edge-case graphs: full level arrays from the reference
+# --------------------------------------------------------------------------
+def test_tiny_graphs_bfs_levels(fastcon_lib, tiny_golden):
+    fc = fastcon_lib
+    for g in tiny_golden:
+        es = np.array(g["edges"], dtype=np.int32).reshape(-1, 2)
+        G = fc.Graph.from_edges(es[:, 0], es[:, 1], g["nv"])
+        rp, col = G.csr()
+        assert rp.tolist() == g["row_ptr"] and col.tolist() == g["col"], g["name"]
+        G2 = fc.Graph.from_csr(np.array(g["row_ptr"]), np.array(g["col"]))
+        for eng in ENGINES_SINGLE:
+            for sch in ("plain", "heuristic"):
+                o = opts(fc, eng, sch)
+                for i, s in enumerate(g["sources"]):
+                    assert G.bfs_levels(s, o).tolist() == g["levels"][i], (g["name"], eng, sch, s)
+                    assert G2.bfs_levels(s, o).tolist() == g["levels"][i]
+
+
+def test_tiny_graphs_stcon_all_pairs(fastcon_lib, tiny_golden):
+    fc = fastcon_lib
+    for g in tiny_golden:
+        es = np.array(g["edges"], dtype=np.int32).reshape(-1, 2)
+        G = fc.Graph.from_edges(es[:, 0], es[:, 1], g["nv"])
+        srcs = g["sources"]
+        ss, tt, want = [], [], []
+        for i, s in enumerate(srcs):
+            for t in range(g["nv"]):
+                ss.append(s)
+                tt.append(t)
+                want.append(g["levels"][i][t])
+        ss, tt, want = np.array(ss), np.array(tt), np.array(want)
+        for eng in ENGINES_SINGLE:
+            for sch in SCHEDS:
+                o = opts(fc, eng, sch)
+                for k in range(0, len(ss), max(1, len(ss) // 40)):
+                    c, h = G.stcon(ss[k], tt[k], o)
+                    assert (c, h) == (want[k] >= 0, want[k]), (g["name"], eng, sch, ss[k], tt[k])
+        for eng in ENGINES_BATCH:
+            for sch in SCHEDS:
+                conn, hops = fc.stcon_batch(G, ss, tt, opts=opts(fc, eng, sch))
+                assert (hops == want).all(), (g["name"], eng, sch)
+                assert (conn == (want >= 0)).all()
+
+
+# --------------------------------------------------------------------------
+# ER workload: 65,536 vertices, 524,288 edges (seed 1), 64 pairs (seed 2)
+# --------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def er_graph(fastcon_lib, er_golden):
+    gi = er_golden["graph"]
+    u, v = graphs.er_edges(gi["n"], gi["m"], seed=gi["seed"])
+    return fastcon_lib.Graph.from_edges(u, v, gi["n"])
+
+
+def test_er_device_ingest_is_canonical(er_graph, er_golden):
+    rp, col = er_graph.csr()
+    assert er_graph.ne == er_golden["graph"]["directed_entries"]
+    assert sha_csr(rp, col) == er_golden["graph"]["csr_sha256"]
+    assert rp.ctypes.data % 4 == 0
+
+
+@pytest.mark.parametrize("engine,sched", [("hostloop", "plain"), ("persistent", "plain"),
+                                          ("persistent", "heuristic"), ("hostloop", "heuristic")])
+def test_er_bfs_levels_match_reference(fastcon_lib, er_graph, er_golden, engine, sched):
+    o = opts(fastcon_lib, engine, sched)
+    bu = 0
+    for i, s in enumerate(er_golden["s"]):
+        lev, st = er_graph.bfs_levels(s, o, stats=True)
+        assert sha_levels(lev) == er_golden["levels_sha256"][i], (engine, sched, s)
+        bu += st["bottom_up_steps"]
+    if sched == "heuristic":
+        assert bu > 0  # the direction switch was exercised
+
+
+@pytest.mark.parametrize("engine", ENGINES_BATCH)
+@pytest.mark.parametrize("sched", SCHEDS)
+def test_er_stcon_matches_reference(fastcon_lib, er_graph, er_golden, engine, sched):
+    s, t = np.array(er_golden["s"]), np.array(er_golden["t"])
+    want = np.array(er_golden["hops"])
+    conn, hops = fastcon_lib.stcon_batch(er_graph, s, t, opts=opts(fastcon_lib, engine, sched))
+    assert (hops == want).all() and (conn == (want >= 0)).all()
+    if engine != "batched":
+        o = opts(fastcon_lib, engine, sched)
+        for k in range(0, 64, 7):
+            assert er_graph.stcon(s[k], t[k], o) == (want[k] >= 0, want[k])
+
+
+# --------------------------------------------------------------------------
+# the reference's known-answer run (Graph500 R-MAT scale 16)
+# --------------------------------------------------------------------------
+def test_known_answer_run(fastcon_lib, ka):
+    fc = fastcon_lib
+    nv, u, v = known_answer_graph()
+    G = fc.Graph.from_edges(u, v, nv)
+    rp, col = G.csr()
+    assert sha_csr(rp, col) == ka["graph"]["csr_sha256"]
+    red = np.array([r["red"] for r in ka["rows"]])
+    blue = np.array([r["blue"] for r in ka["rows"]])
+    depth = [r["depth"] for r in ka["rows"]]
+    for k in range(0, 100, 5):
+        assert G.stcon_depth(red[k], blue[k]) == depth[k]
+    for eng in ENGINES_BATCH:
+        for sch in SCHEDS:
+            conn, hops = fc.stcon_batch(G, red, blue, opts=opts(fc, eng, sch))
+            assert conn.all()
+            assert hops.tolist() == ka["ref_bfs_hops"]
+            assert ((hops + 1) // 2).tolist() == depth
+    for k in range(0, 100, 11):
+        assert sha_levels(G.bfs_levels(red[k])) == ka["ref_bfs_levels_sha256"][k]
+
+
+# --------------------------------------------------------------------------
+# device ingest and generators against the CPU canonical CSR
+# --------------------------------------------------------------------------
+def test_ingest_matches_oracle_csr(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    rng = np.random.default_rng(17)
+    cases = []
+    for nv, n in [(1, 0), (2, 1), (7, 40), (300, 5000), (5000, 60000)]:
+        cases.append((nv, rng.integers(0, nv, n), rng.integers(0, nv, n)))
+    # rows in every sort class: a 20,000-leaf star (large), 3,000 (medium),
+    # with duplicates and loops mixed in
+    hub = np.concatenate([np.zeros(20000), np.full(3000, 1), rng.integers(0, 30000, 3000)])
+    leaf = np.concatenate([rng.permutation(np.arange(2, 20002)), rng.integers(2, 30000, 3000),
+                           rng.integers(0, 30000, 3000)])
+    cases.append((30000, hub, leaf))
+    flagsets = [(0, oracle_mod.CANONICAL),
+                (fc.INGEST_DIRECTED, oracle_mod.DROP_LOOPS | oracle_mod.DEDUPE),
+                (fc.INGEST_KEEP_LOOPS, oracle_mod.SYMMETRIZE | oracle_mod.DEDUPE),
+                (fc.INGEST_KEEP_DUPS, oracle_mod.SYMMETRIZE | oracle_mod.DROP_LOOPS)]
+    for nv, u, v in cases:
+        u = u.astype(np.int32)
+        v = v.astype(np.int32)
+        for ff, of in flagsets:
+            G = fc.Graph.from_edges(u, v, nv, flags=ff)
+            rp, col = G.csr()
+            rp2, col2 = oracle_mod.build_csr(nv, u, v, flags=of)
+            if ff == fc.INGEST_KEEP_DUPS:
+                # duplicates kept: rows must be sorted and equal as multisets
+                assert (rp == rp2).all()
+                for r in range(0, nv, max(1, nv // 200)):
+                    a = col[rp[r]:rp[r + 1]]
+                    assert (np.diff(a) >= 0).all()
+                    assert (a == np.sort(col2[rp2[r]:rp2[r + 1]])).all()
+            else:
+                assert (rp == rp2).all() and (col == col2).all(), (nv, ff)
+
+
+def test_ingest_rejects_bad_ids(fastcon_lib):
+    fc = fastcon_lib
+    with pytest.raises(fc.FastconError) as e:
+        fc.Graph.from_edges(np.array([0, 9]), np.array([1, 1]), 4)
+    assert e.value.code == fc.ERR_INVALID
+
+
+def test_rmat_generator_matches_numpy(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    for scale, ne, seed, perm in [(10, 9000, 3, 4), (12, 8 << 12, 7, -1)]:
+        G = fc.Graph.rmat(scale, ne, seed=seed, perm_seed=perm)
+        u, v = graphs.rmat_edges(scale, ne, seed=seed, perm_seed=None if perm < 0 else perm)
+        rp2, col2 = oracle_mod.build_csr(1 << scale, u, v)
+        rp, col = G.csr()
+        assert (rp == rp2).all() and (col == col2).all()
+
+
+def test_grid_generator_matches_numpy(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    w, h, k = 64, 48, 7
+    G = fc.Graph.grid(w, h, p_del=0.05, del_seed=5, shortcuts=k, sc_seed=6)
+    u, v = graphs.grid_edges(w, h, 0.05, 5, k, 6)
+    rp2, col2 = oracle_mod.build_csr(w * h, u, v)
+    rp, col = G.csr()
+    assert (rp == rp2).all() and (col == col2).all()
+
+
+# --------------------------------------------------------------------------
+# directed graphs: the t side walks the reverse CSR
+# --------------------------------------------------------------------------
+def test_directed_graphs(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    rng = np.random.default_rng(3)
+    nv, n = 2000, 5000
+    u = rng.integers(0, nv, n).astype(np.int32)
+    v = rng.integers(0, nv, n).astype(np.int32)
+    G = fc.Graph.from_edges(u, v, nv, flags=fc.INGEST_DIRECTED)
+    assert G.directed
+    rp, col = oracle_mod.build_csr(nv, u, v, flags=oracle_mod.DROP_LOOPS | oracle_mod.DEDUPE)
+    s, t = graphs.uniform_pairs(nv, 200, seed=9)
+    conn, hops, _ = oracle_mod.stcon_batch(rp, col, s, t)
+    for eng in ENGINES_BATCH:
+        for sch in ("plain", "heuristic"):
+            c2, h2 = fc.stcon_batch(G, s, t, opts=opts(fc, eng, sch))
+            assert (h2 == hops).all() and (c2 == conn).all(), (eng, sch)
+    for k in range(0, 200, 20):
+        lev, _ = oracle_mod.bfs_levels(rp, col, s[k])
+        assert (G.bfs_levels(s[k], opts(fc, "persistent", "heuristic")) == lev).all()
+
+
+# --------------------------------------------------------------------------
+# edge cases
+# --------------------------------------------------------------------------
+def test_edge_cases(fastcon_lib):
+    fc = fastcon_lib
+    G = fc.Graph.from_edges(np.array([0, 1, 3]), np.array([1, 2, 4]), 6)
+    assert G.stcon(2, 2) == (True, 0)
+    assert G.stcon(5, 5) == (True, 0)  # isolated vertex, s == t
+    assert G.stcon(0, 5) == (False, -1)  # isolated target
+    assert G.stcon(5, 0) == (False, -1)  # isolated source
+    assert G.stcon(0, 4) == (False, -1)
+    assert G.stcon(0, 2) == (True, 2)
+    assert G.stcon_depth(0, 2) == 1 and G.stcon_depth(0, 4) == -1 and G.stcon_depth(1, 1) == 0
+    assert G.bfs_levels(5).tolist() == [-1, -1, -1, -1, -1, 0]
+    for bad in [(-1, 0), (0, 6), (6, 6)]:
+        with pytest.raises(fc.FastconError) as e:
+            G.stcon(*bad)
+        assert e.value.code == fc.ERR_INVALID
+    with pytest.raises(fc.FastconError):
+        G.bfs_levels(6)
+    with pytest.raises(fc.FastconError):
+        fc.stcon_batch(G, np.array([0, 1]), np.array([1, 7]))
+    conn, hops = fc.stcon_batch(G, np.zeros(0), np.zeros(0))
+    assert len(conn) == 0 and len(hops) == 0
+    # empty graph (no edges)
+    E = fc.Graph.from_edges(np.zeros(0), np.zeros(0), 3)
+    assert E.ne == 0 and E.stcon(0, 2) == (False, -1) and E.bfs_levels(1).tolist() == [-1, 0, -1]
+
+
+def test_multi_graph_batch(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    Gs, csrs = [], []
+    for k, scale in enumerate([8, 11, 13, 9]):
+        u, v = graphs.rmat_edges(scale, 16 << scale, seed=100 + k, perm_seed=200 + k)
+        Gs.append(fc.Graph.from_edges(u, v, 1 << scale))
+        csrs.append(oracle_mod.build_csr(1 << scale, u, v))
+    rng = np.random.default_rng(1)
+    gi = rng.integers(0, 4, 800).astype(np.int32)
+    s = np.array([rng.integers(0, Gs[g].nv) for g in gi], np.int32)
+    t = np.array([rng.integers(0, Gs[g].nv) for g in gi], np.int32)
+    want = np.zeros(800, np.int32)
+    for g in range(4):
+        m = gi == g
+        _, h, _ = oracle_mod.stcon_batch(*csrs[g], s[m], t[m], nthreads=4)
+        want[m] = h
+    for eng in ENGINES_BATCH:
+        conn, hops = fc.stcon_batch(Gs, s, t, graph_idx=gi, opts=opts(fc, eng, "heuristic"))
+        assert (hops == want).all(), eng
+
+
+def test_batched_many_queries_rmat(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    scale = 16
+    u, v = graphs.rmat_edges(scale, 8 << scale, seed=31, perm_seed=32)
+    G = fc.Graph.from_edges(u, v, 1 << scale)
+    rp, col = G.csr()
+    s, t = graphs.pairs_with_degree(np.diff(rp), 3000, seed=33)
+    _, want, _ = oracle_mod.stcon_batch(rp, col, s, t, nthreads=16)
+    for eng in ("batched", "persistent"):
+        for sch in SCHEDS:
+            conn, hops, st = fc.stcon_batch(G, s, t, opts=opts(fc, eng, sch), stats=True)
+            assert (hops == want).all(), (eng, sch)
+            assert st["edges_inspected"] > 0
