@@ -48,6 +48,9 @@ CONFIGS = {
     "er65536": dict(kind="er", n=65536, m=524288, seed=1, nq=64, qseed=2),
     "grid4096": dict(kind="grid", w=4096, h=4096, p_del=0.05, del_seed=5, sc_seed=6, nq=256,
                      qseed=7, min_manhattan=2000),
+    # smaller R-MAT (same parameters) used for profiler captures
+    "rmat22": dict(kind="rmat", scale=22, edge_samples=8 << 22, seed=3, perm_seed=3, nq=1024,
+                   qseed=4),
 }
 
 
@@ -285,7 +288,9 @@ def run_fastcon(args, cfg):
 
     G, s, t = make_graph_gpu(fc, cfg)
     nq = len(s)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library launches on it and the events record on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     opt = fc.make_opts(sched=fc.SCHED_HEURISTIC, engine=fc.ENGINE_BATCHED,
                        stream=stream.cuda_stream)
     d_s = torch.from_numpy(s).cuda()

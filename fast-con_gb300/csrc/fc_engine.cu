@@ -32,242 +32,10 @@
 #include <vector>
 
 #include "fc_engine.h"
-#include "fc_step.cuh"
+#include "fc_pool.h"
+#include "fc_sched.cuh"
 
 namespace fc {
-
-struct TeamCounters {
-    int tail[2];
-    int found;
-    int err;
-    unsigned long long deg[2];
-    unsigned long long inspected;  // bottom-up adjacency reads
-    int bar[2];
-    int invalid;
-    int pad;
-};
-
-struct GraphPair {
-    DGraph fwd, rev;
-};
-static_assert(sizeof(GraphPair) == sizeof(GraphPairH), "graph table layout");
-
-enum { MODE_BFS = 0, MODE_STCON = 1 };
-enum { DIR_TD = 0, DIR_BU = 1 };
-
-// ---------------------------------------------------------------------------
-// Per-query control state.  Every CTA of a team holds an identical copy; it
-// is advanced from the team's counters after each barrier, so all copies take
-// the same decisions without another barrier.
-// ---------------------------------------------------------------------------
-struct QLocal {
-    int head[2], tail[2];
-    unsigned long long dh[2], dt[2];
-    int radius[2];
-    int steps, bu_steps;
-    unsigned long long inspected, bu_seen, alg_bytes;
-    int done, connected, hops, escalate;
-    int side, dir, variant;
-    int two;
-    int nv;
-    long long ne;
-};
-
-__host__ __device__ inline void ql_start(QLocal &q, int two, int nv, long long ne, int s, int t,
-                                         unsigned long long deg_s, unsigned long long deg_t)
-{
-    q.head[0] = q.head[1] = 0;
-    q.tail[0] = 1;
-    q.tail[1] = (two && s != t) ? 1 : 0;
-    q.dh[0] = q.dh[1] = 0;
-    q.dt[0] = deg_s;
-    q.dt[1] = (two && s != t) ? deg_t : 0;
-    q.radius[0] = q.radius[1] = 0;
-    q.steps = q.bu_steps = 0;
-    q.inspected = q.bu_seen = q.alg_bytes = 0;
-    q.done = 0;
-    q.connected = 0;
-    q.hops = -1;
-    q.escalate = 0;
-    q.side = 0;
-    q.dir = DIR_TD;
-    q.variant = 0;
-    q.two = two;
-    q.nv = nv;
-    q.ne = ne;
-    if (two && s == t) {
-        q.done = 1;
-        q.connected = 1;
-        q.hops = 0;
-    }
-}
-
-// Choose the next step.  allow_bu = 0 in the batched engine (a bottom-up step
-// scans every vertex, which one CTA must not do).  bu_level_cap limits
-// bottom-up to levels whose status code is exact (s-t status bytes hold
-// min(level, 127)).
-__host__ __device__ inline void ql_decide(QLocal &q, int sched, int allow_bu, int bu_level_cap)
-{
-    int side;
-    if (!q.two)
-        side = 0;
-    else if (sched == FC_SCHED_PLAIN)
-        side = q.steps & 1;
-    else {
-        unsigned long long m0 = q.dt[0] - q.dh[0], m1 = q.dt[1] - q.dh[1];
-        side = m0 <= m1 ? 0 : 1;
-    }
-    q.side = side;
-    q.dir = DIR_TD;
-    q.variant = 0;
-    if (sched != FC_SCHED_PLAIN && allow_bu && q.radius[side] + 1 <= bu_level_cap) {
-        long long mf = (long long)(q.dt[side] - q.dh[side]);
-        long long unexplored = q.ne - (long long)(q.dt[0] + q.dt[1]);
-        long long nf = q.tail[side] - q.head[side];
-        // Beamer, Asanovic & Patterson (SC'12) thresholds: alpha = 14, beta = 24
-        if (mf * 14 > unexplored && nf * 24 > q.nv) q.dir = DIR_BU;
-    }
-}
-
-// Advance after the step on q.side finished (counters final).
-__host__ __device__ inline void ql_update(QLocal &q, int found, int tail_x,
-                                          unsigned long long deg_x, unsigned long long bu_total)
-{
-    const int x = q.side;
-    // algorithmic bytes of the step (4-byte status words, 8 bytes per row
-    // range, 4 per column entry and per queue entry):
-    //   top-down   4|F| + 8|F| + 4 E_F + 4 E_F + 4|N| + 4|N|
-    //   bottom-up  sum over scanned v of (4 + 8 + 8 k_v), plus 8|N|
-    const unsigned long long nnew = (unsigned long long)(tail_x - q.tail[x]);
-    if (q.dir == DIR_TD) {
-        const unsigned long long ef = q.dt[x] - q.dh[x];
-        const unsigned long long nf = (unsigned long long)(q.tail[x] - q.head[x]);
-        q.inspected += ef;
-        q.alg_bytes += 12ull * nf + 8ull * ef + 8ull * nnew;
-    } else {
-        const unsigned long long k = bu_total - q.bu_seen;
-        q.inspected += k;
-        q.alg_bytes += 12ull * (unsigned long long)q.nv + 8ull * k + 8ull * nnew;
-        q.bu_steps++;
-    }
-    q.bu_seen = bu_total;
-    q.steps++;
-    if (found && q.two) {
-        q.done = 1;
-        q.connected = 1;
-        q.hops = q.radius[x] + 1 + q.radius[1 - x];
-    }
-    q.head[x] = q.tail[x];
-    q.tail[x] = tail_x;
-    q.dh[x] = q.dt[x];
-    q.dt[x] = deg_x;
-    q.radius[x]++;
-    if (!q.done && q.tail[x] == q.head[x]) {
-        q.done = 1;
-        q.connected = 0;
-        q.hops = -1;
-    }
-}
-
-__device__ __forceinline__ const int32_t *ql_frontier(const QLocal &q, const int32_t *log, int cap,
-                                                     int x, int *F)
-{
-    *F = q.tail[x] - q.head[x];
-    return x == 0 ? log + q.head[0] : log + (cap - q.tail[1]);
-}
-
-// ---------------------------------------------------------------------------
-// One step for a team of CTAs.
-// ---------------------------------------------------------------------------
-template <int T>
-__device__ void run_step(int mode, const GraphPair &gp, int side, int dir, int level,
-                         int other_radius, const int32_t *frontier, int F, int team_rank,
-                         int team_size, uint8_t *status, int32_t *levels, int32_t *log, int cap,
-                         int *tail_ctr, unsigned long long *deg_ctr, int *found,
-                         unsigned long long *bu_ins, SmemTopDown<T> &sm)
-{
-    const DGraph &gx = side ? gp.rev : gp.fwd;
-    AppendTarget app{log, cap, side, tail_ctr, deg_ctr, gx.row_ptr};
-    if (dir == DIR_TD) {
-        if (mode == MODE_BFS) {
-            VisitBFS vis{levels, level + 1};
-            topdown_step<T>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis, app, sm,
-                            nullptr);
-        } else {
-            VisitSTCON vis{status, st_code(side, level + 1), side, found};
-            topdown_step<T>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis, app, sm,
-                            found);
-        }
-    } else {
-        const DGraph &gr = side ? gp.fwd : gp.rev;
-        if (mode == MODE_BFS) {
-            BottomUpBFS bu{levels, level};
-            bottomup_step<T>(gr.row_ptr, gr.col, gr.nv, team_rank, team_size, bu, app, bu_ins);
-        } else {
-            BottomUpSTCON bu{status, st_code(side, level), st_code(side, level + 1),
-                             st_code(1 - side, other_radius), found};
-            bottomup_step<T>(gr.row_ptr, gr.col, gr.nv, team_rank, team_size, bu, app, bu_ins);
-        }
-    }
-}
-
-// Root initialisation (one thread).  Writes the counters, the roots' status
-// (or level) and their log entries.
-__device__ void init_roots(int mode, const GraphPair &gp, int s, int t, uint8_t *status,
-                           int32_t *levels, int32_t *log, int cap, TeamCounters *tc)
-{
-    tc->found = 0;
-    tc->inspected = 0;
-    tc->invalid = 0;
-    if (mode == MODE_BFS) {
-        levels[s] = 0;
-        log[0] = s;
-        tc->tail[0] = 1;
-        tc->tail[1] = 0;
-        tc->deg[0] = (unsigned long long)(gp.fwd.row_ptr[s + 1] - gp.fwd.row_ptr[s]);
-        tc->deg[1] = 0;
-        return;
-    }
-    status[s] = st_code(0, 0);
-    log[0] = s;
-    tc->tail[0] = 1;
-    tc->deg[0] = (unsigned long long)(gp.fwd.row_ptr[s + 1] - gp.fwd.row_ptr[s]);
-    if (s != t) {
-        status[t] = st_code(1, 0);
-        log[cap - 1] = t;
-        tc->tail[1] = 1;
-        tc->deg[1] = (unsigned long long)(gp.rev.row_ptr[t + 1] - gp.rev.row_ptr[t]);
-    } else {
-        tc->tail[1] = 0;
-        tc->deg[1] = 0;
-        tc->found = 1;
-    }
-}
-
-__device__ __forceinline__ void write_result(int q, const QLocal &ql, int32_t *out_conn,
-                                             int32_t *out_hops, QueryStat *qs, int escalated)
-{
-    if (!escalated) {
-        if (out_conn) out_conn[q] = ql.connected;
-        if (out_hops) out_hops[q] = ql.hops;
-    }
-    if (qs) {
-        QueryStat r;
-        r.inspected = (long long)ql.inspected;
-        r.alg_bytes = (long long)ql.alg_bytes;
-        r.steps = ql.steps;
-        r.bu_steps = ql.bu_steps;
-        r.visited = ql.tail[0] + ql.tail[1];
-        r.escalated = escalated;
-        if (escalated) {
-            // the persistent engine rewrites the record; keep the CTA's part
-            qs[q].escalated = 1;
-        } else {
-            r.escalated = qs[q].escalated;
-            qs[q] = r;
-        }
-    }
-}
 
 // ---------------------------------------------------------------------------
 // host-loop engine kernels
@@ -380,99 +148,6 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
     }
 }
 
-// ---------------------------------------------------------------------------
-// batched engine: one CTA per query at a time, private slot per CTA.
-// ---------------------------------------------------------------------------
-struct BatchArgs {
-    const GraphPair *graphs;
-    const int32_t *graph_idx;
-    const int32_t *qs;
-    const int32_t *qt;
-    int nq;
-    int *ctr;  // [0] next query, [1] spill count, [2] invalid flag
-    int32_t *spill;
-    uint8_t *status_arena;
-    size_t status_stride;
-    int32_t *log_arena;
-    size_t log_stride;
-    int log_cap;
-    long long work_limit;
-    int sched;
-    int32_t *out_conn;
-    int32_t *out_hops;
-    QueryStat *qstat;
-};
-
-template <int T>
-__global__ void __launch_bounds__(T) k_batched(BatchArgs a)
-{
-    __shared__ SmemTopDown<T> sm;
-    __shared__ QLocal ql;
-    __shared__ TeamCounters tc;
-    __shared__ int s_q;
-    uint8_t *status = a.status_arena + (size_t)blockIdx.x * a.status_stride;
-    int32_t *log = a.log_arena + (size_t)blockIdx.x * a.log_stride;
-    const int cap = a.log_cap;
-    while (true) {
-        if (threadIdx.x == 0) s_q = atomicAdd(&a.ctr[0], 1);
-        __syncthreads();
-        const int q = s_q;
-        if (q >= a.nq) break;
-        const GraphPair gp = a.graphs[a.graph_idx ? a.graph_idx[q] : 0];
-        const int nv = gp.fwd.nv;
-        const int s = a.qs[q], t = a.qt[q];
-        if (s < 0 || s >= nv || t < 0 || t >= nv) {
-            if (threadIdx.x == 0) {
-                if (a.out_conn) a.out_conn[q] = 0;
-                if (a.out_hops) a.out_hops[q] = -2;
-                a.ctr[2] = 1;
-            }
-            __syncthreads();
-            continue;
-        }
-        if (threadIdx.x == 0) {
-            init_roots(MODE_STCON, gp, s, t, status, nullptr, log, cap, &tc);
-            ql_start(ql, 1, nv, gp.fwd.ne, s, t, tc.deg[0], tc.deg[1]);
-        }
-        __syncthreads();
-        while (true) {
-            if (threadIdx.x == 0 && !ql.done) {
-                ql_decide(ql, a.sched, 0, LEVEL7_MAX);
-                const int x = ql.side;
-                long long mf = (long long)(ql.dt[x] - ql.dh[x]);
-                if (mf > a.work_limit || (long long)ql.tail[0] + ql.tail[1] + mf > cap) {
-                    ql.escalate = 1;
-                    ql.done = 1;
-                }
-            }
-            __syncthreads();
-            if (ql.done) break;
-            int F;
-            const int x = ql.side;
-            const int32_t *front = ql_frontier(ql, log, cap, x, &F);
-            run_step<T>(MODE_STCON, gp, x, DIR_TD, ql.radius[x], ql.radius[1 - x], front, F, 0, 1,
-                        status, nullptr, log, cap, &tc.tail[x], &tc.deg[x], &tc.found,
-                        &tc.inspected, sm);
-            __syncthreads();
-            if (threadIdx.x == 0) ql_update(ql, tc.found, tc.tail[x], tc.deg[x], tc.inspected);
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) {
-            if (ql.escalate) {
-                int k = atomicAdd(&a.ctr[1], 1);
-                a.spill[k] = q;
-            }
-            write_result(q, ql, a.out_conn, a.out_hops, a.qstat, ql.escalate);
-        }
-        const int n0 = ql.tail[0], n1 = ql.tail[1];
-        for (int i = threadIdx.x; i < n0 + n1; i += T) {
-            int v = i < n0 ? log[i] : log[cap - 1 - (i - n0)];
-            status[v] = ST_UNVISITED;
-        }
-        __syncthreads();
-    }
-}
-
 // ===========================================================================
 // host side
 // ===========================================================================
@@ -531,7 +206,7 @@ DevCtx *get_ctx(int *err)
             cudaEventCreate(&c->evm) != cudaSuccess ||
             cudaMalloc(&c->tc, sizeof(TeamCounters)) != cudaSuccess ||
             cudaMallocHost(&c->h_tc, sizeof(TeamCounters)) != cudaSuccess ||
-            cudaMalloc(&c->b_ctr, 4 * sizeof(int)) != cudaSuccess) {
+            cudaMalloc(&c->b_ctr, 8 * sizeof(int)) != cudaSuccess) {
             *err = FC_ERR_CUDA;
             set_error("device context set-up failed");
             return nullptr;
@@ -681,19 +356,154 @@ static void fill_stats(fc_stats *st, const QLocal &q, int launches)
     st->launches = launches;
 }
 
-static void from_qstat(QLocal &q, const QueryStat &h)
+static void accumulate(QLocal &tot, const QueryStat &h)
 {
-    q.inspected = (unsigned long long)h.inspected;
-    q.alg_bytes = (unsigned long long)h.alg_bytes;
-    q.steps = h.steps;
-    q.bu_steps = h.bu_steps;
-    q.tail[0] = h.visited;
-    q.tail[1] = 0;
+    tot.inspected += (unsigned long long)h.inspected;
+    tot.alg_bytes += (unsigned long long)h.alg_bytes;
+    tot.tail[0] += h.visited;
+    tot.steps += h.steps;
+    tot.bu_steps += h.bu_steps;
+}
+
+static int ensure_qstat(DevCtx *c, size_t n)
+{
+    if (n <= c->qstat_cap && c->qstat) return FC_OK;
+    cudaFree(c->qstat);
+    c->qstat = nullptr;
+    c->qstat_cap = 0;
+    size_t cap = n < 1024 ? 1024 : n;
+    FC_CUDA_TRY(cudaMalloc(&c->qstat, sizeof(QueryStat) * cap));
+    c->qstat_cap = cap;
+    return FC_OK;
+}
+
+static int ensure_tmp(DevCtx *c)
+{
+    if (c->d_tmp_q) return FC_OK;
+    FC_CUDA_TRY(cudaMalloc(&c->d_tmp_q, sizeof(int32_t) * 4096));
+    c->tmp_q_cap = 4096;
+    return FC_OK;
+}
+
+// per-CTA slot records of the pool engine, sized for the largest grid
+static int ensure_pool(DevCtx *c)
+{
+    if (c->p_slots) return FC_OK;
+    int grid = pool_grid(c->sm_count, 0);
+    if (grid <= 0 || !c->coop) {
+        set_error("cooperative launch unavailable for the pool engine");
+        return FC_ERR_UNSUPPORTED;
+    }
+    FC_CUDA_TRY(cudaMalloc(&c->p_slots, pool_slot_bytes() * (size_t)grid));
+    FC_CUDA_TRY(cudaMalloc(&c->p_jobs, pool_job_bytes() * (size_t)grid));
+    FC_CUDA_TRY(cudaMemset(c->p_slots, 0, pool_slot_bytes() * (size_t)grid));
+    FC_CUDA_TRY(cudaMemset(c->p_jobs, 0, pool_job_bytes() * (size_t)grid));
+    c->p_grid = grid;
+    return FC_OK;
+}
+
+static int check_pool(DevCtx *c, cudaStream_t st, int *invalid)
+{
+    int h[8];
+    FC_CUDA_TRY(cudaMemcpyAsync(h, c->b_ctr, sizeof(h), cudaMemcpyDeviceToHost, st));
+    FC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (invalid) *invalid = h[4];
+    if (h[3]) {
+        set_error("device-side wait timed out in the pool engine");
+        // leave every workspace clean for the next call
+        cudaMemset(c->p_slots, 0, pool_slot_bytes() * (size_t)c->p_grid);
+        if (c->status) cudaMemset(c->status, 0xFF, (c->ws_nv + 15) / 16 * 16);
+        if (c->b_status) cudaMemset(c->b_status, 0xFF, c->b_slots * c->b_status_stride);
+        return FC_ERR_TIMEOUT;
+    }
+    return FC_OK;
+}
+
+static long long private_edges_default(const fc_opts &o, bool exclusive)
+{
+    // exclusive (one query at a time): share every step that has work for
+    // more than a few CTAs; batched: keep steps private up to the CTA limit;
+    // a negative setting shares every step
+    if (o.cta_work_k < 0) return 0;
+    if (o.cta_work_k > 0) return (long long)o.cta_work_k * 1024;
+    return exclusive ? 4096 : 16 * 1024;
+}
+
+static PoolArgs pool_args_exclusive(DevCtx *c, int mode, const fc_opts &o)
+{
+    PoolArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.graphs = (const GraphPair *)c->d_graphs;
+    a.mode = mode;
+    a.sched = o.sched;
+    a.exclusive = 1;
+    a.slots = (PoolSlot *)c->p_slots;
+    a.jobs = (RowJob *)c->p_jobs;
+    a.status_base = c->status;
+    a.levels = c->levels;
+    a.log_base = c->log;
+    a.log_cap = (int)c->ws_nv;
+    a.private_edges = private_edges_default(o, true);
+    a.ctr = c->b_ctr;
+    a.qstat = c->qstat;
+    return a;
 }
 
 static int pick_engine(const fc_opts &o, int dflt)
 {
     return o.engine == FC_ENGINE_AUTO ? dflt : o.engine;
+}
+
+// one query (BFS levels or s-t) on the persistent grid-barrier engine or the
+// pool engine in exclusive mode; results land in c->d_tmp_q[2..3]
+static int run_single(DevCtx *c, int mode, int engine, const GraphPairH &gp, int32_t s, int32_t t,
+                      const fc_opts &o, QLocal &q, cudaStream_t stream)
+{
+    int rc = ensure_graphs(c, &gp, 1, stream);
+    if (rc) return rc;
+    if ((rc = ensure_qstat(c, 1)) || (rc = ensure_tmp(c))) return rc;
+    int32_t hq[2] = {s, t};
+    FC_CUDA_TRY(cudaMemcpyAsync(c->d_tmp_q, hq, sizeof(hq), cudaMemcpyHostToDevice, stream));
+    FC_CUDA_TRY(cudaMemsetAsync(c->qstat, 0, sizeof(QueryStat), stream));
+    if (engine == FC_ENGINE_PERSISTENT) {
+        PersistArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.graphs = (const GraphPair *)c->d_graphs;
+        a.qs = c->d_tmp_q;
+        a.qt = c->d_tmp_q + 1;
+        a.nlist = 1;
+        a.mode = mode;
+        a.sched = o.sched;
+        a.status = c->status;
+        a.levels = c->levels;
+        a.log = c->log;
+        a.tc = c->tc;
+        a.out_conn = c->d_tmp_q + 2;
+        a.out_hops = c->d_tmp_q + 3;
+        a.qstat = c->qstat;
+        rc = launch_persistent<FC_BLOCK>(c, a, stream);
+        if (rc) return rc;
+        rc = check_counters(c, stream);
+        if (rc) return rc;
+    } else {
+        if ((rc = ensure_pool(c))) return rc;
+        FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 8 * sizeof(int), stream));
+        PoolArgs a = pool_args_exclusive(c, mode, o);
+        a.qs = c->d_tmp_q;
+        a.qt = c->d_tmp_q + 1;
+        a.nlist = 1;
+        a.out_conn = c->d_tmp_q + 2;
+        a.out_hops = c->d_tmp_q + 3;
+        rc = pool_launch(a, c->p_grid, stream);
+        if (rc) return rc;
+        rc = check_pool(c, stream, nullptr);
+        if (rc) return rc;
+    }
+    QueryStat h;
+    FC_CUDA_TRY(cudaMemcpy(&h, c->qstat, sizeof(h), cudaMemcpyDeviceToHost));
+    std::memset(&q, 0, sizeof(q));
+    accumulate(q, h);
+    return FC_OK;
 }
 
 int engine_bfs(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_levels, const fc_opts &o,
@@ -704,52 +514,15 @@ int engine_bfs(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_levels, co
     if (rc) return rc;
     FC_CUDA_TRY(cudaMemsetAsync(c->levels, 0xFF, sizeof(int32_t) * (size_t)nv, stream));
     FC_CUDA_TRY(cudaEventRecord(c->ev0, stream));
-    const int engine = pick_engine(o, FC_ENGINE_PERSISTENT);
+    const int engine = pick_engine(o, FC_ENGINE_BATCHED);
     QLocal q;
     std::memset(&q, 0, sizeof(q));
     if (engine == FC_ENGINE_HOSTLOOP) {
         rc = hostloop(c, MODE_BFS, gp, s, s, o.sched, &q, stream);
-        if (rc) return rc;
     } else {
-        rc = ensure_graphs(c, &gp, 1, stream);
-        if (rc) return rc;
-        QueryStat *qs = nullptr;
-        if (c->qstat_cap < 1) {
-            FC_CUDA_TRY(cudaMalloc(&c->qstat, sizeof(QueryStat) * 1024));
-            c->qstat_cap = 1024;
-        }
-        qs = c->qstat;
-        FC_CUDA_TRY(cudaMemsetAsync(qs, 0, sizeof(QueryStat), stream));
-        int32_t *d_s = nullptr;
-        if (c->tmp_q_cap < 4) {
-            cudaFree(c->d_tmp_q);
-            c->d_tmp_q = nullptr;
-            FC_CUDA_TRY(cudaMalloc(&c->d_tmp_q, sizeof(int32_t) * 4096));
-            c->tmp_q_cap = 4096;
-        }
-        d_s = c->d_tmp_q;
-        FC_CUDA_TRY(cudaMemcpyAsync(d_s, &s, sizeof(int32_t), cudaMemcpyHostToDevice, stream));
-        PersistArgs a;
-        std::memset(&a, 0, sizeof(a));
-        a.graphs = (const GraphPair *)c->d_graphs;
-        a.qs = d_s;
-        a.qt = d_s;
-        a.nlist = 1;
-        a.mode = MODE_BFS;
-        a.sched = o.sched;
-        a.status = c->status;
-        a.levels = c->levels;
-        a.log = c->log;
-        a.tc = c->tc;
-        a.qstat = qs;
-        rc = launch_persistent<FC_BLOCK>(c, a, stream);
-        if (rc) return rc;
-        rc = check_counters(c, stream);
-        if (rc) return rc;
-        QueryStat h;
-        FC_CUDA_TRY(cudaMemcpy(&h, qs, sizeof(h), cudaMemcpyDeviceToHost));
-        from_qstat(q, h);
+        rc = run_single(c, MODE_BFS, engine, gp, s, s, o, q, stream);
     }
+    if (rc) return rc;
     FC_CUDA_TRY(cudaEventRecord(c->ev1, stream));
     if (h_levels)
         FC_CUDA_TRY(cudaMemcpyAsync(h_levels, c->levels, sizeof(int32_t) * (size_t)nv,
@@ -771,7 +544,7 @@ int engine_stcon(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int32_t 
     int rc = ensure_ws(c, (size_t)nv);
     if (rc) return rc;
     FC_CUDA_TRY(cudaEventRecord(c->ev0, stream));
-    const int engine = pick_engine(o, FC_ENGINE_PERSISTENT);
+    const int engine = pick_engine(o, FC_ENGINE_BATCHED);
     QLocal q;
     std::memset(&q, 0, sizeof(q));
     if (engine == FC_ENGINE_HOSTLOOP) {
@@ -781,50 +554,13 @@ int engine_stcon(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int32_t 
         FC_CUDA_TRY(cudaMemsetAsync(c->status, 0xFF, (size_t)(nv + 15) / 16 * 16, stream));
         *conn = q.connected;
         *hops = q.hops;
-    } else if (engine == FC_ENGINE_PERSISTENT || engine == FC_ENGINE_BATCHED) {
-        rc = ensure_graphs(c, &gp, 1, stream);
-        if (rc) return rc;
-        if (c->qstat_cap < 1) {
-            FC_CUDA_TRY(cudaMalloc(&c->qstat, sizeof(QueryStat) * 1024));
-            c->qstat_cap = 1024;
-        }
-        if (c->tmp_q_cap < 4) {
-            cudaFree(c->d_tmp_q);
-            c->d_tmp_q = nullptr;
-            FC_CUDA_TRY(cudaMalloc(&c->d_tmp_q, sizeof(int32_t) * 4096));
-            c->tmp_q_cap = 4096;
-        }
-        int32_t hq[2] = {s, t};
-        FC_CUDA_TRY(cudaMemcpyAsync(c->d_tmp_q, hq, sizeof(hq), cudaMemcpyHostToDevice, stream));
-        FC_CUDA_TRY(cudaMemsetAsync(c->qstat, 0, sizeof(QueryStat), stream));
-        PersistArgs a;
-        std::memset(&a, 0, sizeof(a));
-        a.graphs = (const GraphPair *)c->d_graphs;
-        a.qs = c->d_tmp_q;
-        a.qt = c->d_tmp_q + 1;
-        a.nlist = 1;
-        a.mode = MODE_STCON;
-        a.sched = o.sched;
-        a.status = c->status;
-        a.levels = c->levels;
-        a.log = c->log;
-        a.tc = c->tc;
-        a.out_conn = c->d_tmp_q + 2;
-        a.out_hops = c->d_tmp_q + 3;
-        a.qstat = c->qstat;
-        rc = launch_persistent<FC_BLOCK>(c, a, stream);
-        if (rc) return rc;
-        rc = check_counters(c, stream);
+    } else {
+        rc = run_single(c, MODE_STCON, engine, gp, s, t, o, q, stream);
         if (rc) return rc;
         int32_t res[2];
         FC_CUDA_TRY(cudaMemcpy(res, c->d_tmp_q + 2, sizeof(res), cudaMemcpyDeviceToHost));
-        QueryStat h;
-        FC_CUDA_TRY(cudaMemcpy(&h, c->qstat, sizeof(h), cudaMemcpyDeviceToHost));
         *conn = res[0];
         *hops = res[1];
-        from_qstat(q, h);
-    } else {
-        return FC_ERR_UNSUPPORTED;
     }
     FC_CUDA_TRY(cudaEventRecord(c->ev1, stream));
     FC_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -838,7 +574,7 @@ int engine_stcon(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int32_t 
 }
 
 // ---------------------------------------------------------------------------
-// batched engine host side
+// batches
 // ---------------------------------------------------------------------------
 static int ensure_batch_arena(DevCtx *c, size_t slots, size_t maxnv, int log_cap)
 {
@@ -870,22 +606,13 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
     constexpr int T = FC_BLOCK;
     if (nq <= 0) return FC_OK;
     size_t maxnv = 1;
-    long long max_ne = 0;
-    for (int i = 0; i < ngraphs; ++i) {
+    for (int i = 0; i < ngraphs; ++i)
         if ((size_t)gps[i].fwd.nv > maxnv) maxnv = (size_t)gps[i].fwd.nv;
-        if (gps[i].fwd.ne > max_ne) max_ne = gps[i].fwd.ne;
-    }
     int rc = ensure_ws(c, maxnv);
     if (rc) return rc;
     rc = ensure_graphs(c, gps, ngraphs, stream);
     if (rc) return rc;
-    if ((size_t)nq > c->qstat_cap) {
-        cudaFree(c->qstat);
-        c->qstat = nullptr;
-        c->qstat_cap = 0;
-        FC_CUDA_TRY(cudaMalloc(&c->qstat, sizeof(QueryStat) * (size_t)nq));
-        c->qstat_cap = (size_t)nq;
-    }
+    if ((rc = ensure_qstat(c, (size_t)nq))) return rc;
     if ((size_t)nq > c->b_spill_cap) {
         cudaFree(c->b_spill);
         c->b_spill = nullptr;
@@ -894,64 +621,61 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         c->b_spill_cap = (size_t)nq;
     }
     const int engine = pick_engine(o, FC_ENGINE_BATCHED);
+    int launches = 0;
     FC_CUDA_TRY(cudaEventRecord(c->ev0, stream));
     FC_CUDA_TRY(cudaMemsetAsync(c->qstat, 0, sizeof(QueryStat) * (size_t)nq, stream));
-    FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 4 * sizeof(int), stream));
+    FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 8 * sizeof(int), stream));
     if (engine == FC_ENGINE_BATCHED) {
-        int per_sm = o.ctas_per_sm;
-        if (per_sm <= 0) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batched<T>, T, 0);
-            if (per_sm > 4) per_sm = 4;
-        }
-        if (per_sm < 1) per_sm = 1;
-        size_t slots = (size_t)per_sm * (size_t)c->sm_count;
-        if (o.max_slots > 0 && (size_t)o.max_slots < slots) slots = (size_t)o.max_slots;
-        if (slots > (size_t)nq) slots = (size_t)nq;
-        // log space per slot: enough for the CTA work limit
-        const long long work_limit = 1ll << 20;
-        int log_cap = (int)std::min<size_t>(maxnv, (size_t)(2 * work_limit + 1024));
-        rc = ensure_batch_arena(c, slots, maxnv, log_cap);
+        if ((rc = ensure_pool(c))) return rc;
+        int grid = pool_grid(c->sm_count, o.ctas_per_sm);
+        if (grid > c->p_grid) grid = c->p_grid;
+        if (o.max_slots > 0 && o.max_slots < grid) grid = o.max_slots;
+        // a slot's visit log bounds the queries it can finish itself; bigger
+        // ones move to the exclusive pass below
+        int log_cap = (int)std::min<size_t>(maxnv, (size_t)1 << 22);
+        rc = ensure_batch_arena(c, (size_t)grid, maxnv, log_cap);
         if (rc) return rc;
-        BatchArgs b;
-        b.graphs = (const GraphPair *)c->d_graphs;
-        b.graph_idx = d_gi;
-        b.qs = d_s;
-        b.qt = d_t;
-        b.nq = nq;
-        b.ctr = c->b_ctr;
-        b.spill = c->b_spill;
-        b.status_arena = c->b_status;
-        b.status_stride = c->b_status_stride;
-        b.log_arena = c->b_log;
-        b.log_stride = c->b_log_stride;
-        b.log_cap = log_cap;
-        b.work_limit = work_limit;
-        b.sched = o.sched == FC_SCHED_PLAIN ? FC_SCHED_HEURISTIC : o.sched;
-        b.out_conn = d_conn;
-        b.out_hops = d_hops;
-        b.qstat = c->qstat;
-        k_batched<T><<<(unsigned)slots, T, 0, stream>>>(b);
-        FC_CUDA_TRY(cudaGetLastError());
-        FC_CUDA_TRY(cudaEventRecord(c->evm, stream));
-        PersistArgs a;
+        PoolArgs a;
         std::memset(&a, 0, sizeof(a));
         a.graphs = (const GraphPair *)c->d_graphs;
         a.graph_idx = d_gi;
         a.qs = d_s;
         a.qt = d_t;
-        a.list = c->b_spill;
-        a.list_count = c->b_ctr + 1;
+        a.nlist = nq;
         a.mode = MODE_STCON;
-        a.sched = o.sched == FC_SCHED_PLAIN ? FC_SCHED_HEURISTIC : o.sched;
-        a.status = c->status;
-        a.levels = c->levels;
-        a.log = c->log;
-        a.tc = c->tc;
+        a.sched = o.sched;
+        a.exclusive = 0;
+        a.slots = (PoolSlot *)c->p_slots;
+        a.jobs = (RowJob *)c->p_jobs;
+        a.status_base = c->b_status;
+        a.status_stride = c->b_status_stride;
+        a.log_base = c->b_log;
+        a.log_stride = c->b_log_stride;
+        a.log_cap = log_cap;
+        a.private_edges = private_edges_default(o, false);
+        a.ctr = c->b_ctr;
+        a.spill = c->b_spill;
         a.out_conn = d_conn;
         a.out_hops = d_hops;
         a.qstat = c->qstat;
-        rc = launch_persistent<T>(c, a, stream);
+        rc = pool_launch(a, grid, stream);
         if (rc) return rc;
+        FC_CUDA_TRY(cudaEventRecord(c->evm, stream));
+        // queries whose visit log outgrew their slot: one at a time, whole grid
+        PoolArgs x = pool_args_exclusive(c, MODE_STCON, o);
+        x.graph_idx = d_gi;
+        x.qs = d_s;
+        x.qt = d_t;
+        x.list = c->b_spill;
+        x.list_count = c->b_ctr + 2;
+        x.out_conn = d_conn;
+        x.out_hops = d_hops;
+        // same counter block: next and finished restart at 0, the spill count
+        // ([2]) and the error / invalid flags carry over
+        FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 2 * sizeof(int), stream));
+        rc = pool_launch(x, c->p_grid, stream);
+        if (rc) return rc;
+        launches = 2;
     } else if (engine == FC_ENGINE_PERSISTENT) {
         PersistArgs a;
         std::memset(&a, 0, sizeof(a));
@@ -971,6 +695,8 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.qstat = c->qstat;
         rc = launch_persistent<T>(c, a, stream);
         if (rc) return rc;
+        FC_CUDA_TRY(cudaEventRecord(c->evm, stream));
+        launches = 1;
     } else if (engine == FC_ENGINE_HOSTLOOP) {
         // the plain form: one host-driven query at a time
         std::vector<int32_t> hs(nq), ht(nq), hg(nq, 0), hc(nq), hh(nq);
@@ -1009,6 +735,8 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
             float ms = 0;
             cudaEventElapsedTime(&ms, c->ev0, c->ev1);
             st->gpu_ms = ms;
+            st->kernel_ms[0] = ms;
+            st->kernel_alg_bytes[0] = (int64_t)tot.alg_bytes;
         }
         return FC_OK;
     } else {
@@ -1016,7 +744,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
     }
     FC_CUDA_TRY(cudaEventRecord(c->ev1, stream));
     if (sync || st) {
-        rc = check_counters(c, stream);
+        rc = engine == FC_ENGINE_PERSISTENT ? check_counters(c, stream) : check_pool(c, stream, nullptr);
         if (rc) return rc;
     }
     if (st) {
@@ -1027,32 +755,21 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         long long bytes_k[2] = {0, 0};
         int esc = 0;
         for (int i = 0; i < nq; ++i) {
-            tot.inspected += (unsigned long long)h[i].inspected;
-            tot.alg_bytes += (unsigned long long)h[i].alg_bytes;
-            tot.tail[0] += h[i].visited;
-            tot.steps += h[i].steps;
-            tot.bu_steps += h[i].bu_steps;
+            accumulate(tot, h[i]);
             esc += h[i].escalated;
             bytes_k[h[i].escalated ? 1 : 0] += h[i].alg_bytes;
         }
-        const bool batched = engine == FC_ENGINE_BATCHED;
-        fill_stats(st, tot, batched ? 2 : 1);
+        fill_stats(st, tot, launches);
         st->escalated = esc;
-        float ms = 0;
+        float ms = 0, m0 = 0, m1 = 0;
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        cudaEventElapsedTime(&m0, c->ev0, c->evm);
+        cudaEventElapsedTime(&m1, c->evm, c->ev1);
         st->gpu_ms = ms;
-        if (batched) {
-            float m0 = 0, m1 = 0;
-            cudaEventElapsedTime(&m0, c->ev0, c->evm);
-            cudaEventElapsedTime(&m1, c->evm, c->ev1);
-            st->kernel_ms[0] = m0;
-            st->kernel_ms[1] = m1;
-            st->kernel_alg_bytes[0] = bytes_k[0];
-            st->kernel_alg_bytes[1] = bytes_k[1];
-        } else {
-            st->kernel_ms[1] = ms;
-            st->kernel_alg_bytes[1] = bytes_k[0] + bytes_k[1];
-        }
+        st->kernel_ms[0] = m0;
+        st->kernel_ms[1] = m1;
+        st->kernel_alg_bytes[0] = bytes_k[0];
+        st->kernel_alg_bytes[1] = bytes_k[1];
     }
     return FC_OK;
 }

@@ -53,6 +53,10 @@ struct DevCtx {
     uint8_t *b_status = nullptr;
     int32_t *b_log = nullptr;
     size_t b_slots = 0, b_status_stride = 0, b_log_stride = 0;
+    // pool engine: one slot record and one row-job area per resident CTA
+    void *p_slots = nullptr;
+    void *p_jobs = nullptr;
+    int p_grid = 0;
     int b_log_cap = 0;
     int *b_ctr = nullptr;            // [0] next query, [1] spill count, [2] error
     int32_t *b_spill = nullptr;

@@ -1,0 +1,518 @@
+// fc_pool.cu -- the work-sharing ("pool") engine: many s-t queries (or one
+// BFS) per cooperative launch, with no host round trip and no grid barrier.
+//
+// Every CTA owns a slot (status bytes, visit log) and pulls queries from a
+// global counter; small steps run privately inside the CTA with __syncthreads
+// between levels (the one-CTA-per-source shape of BFS_4K_BLOCK,
+// BFS_4K_BLOCK/.../BFS_WE_Block.cu:33-147).  A step whose frontier reads more
+// than `private_edges` adjacency entries, every bottom-up step, and every step
+// of a query run in exclusive mode is *published*: its work is cut into tiles
+// (256 frontier vertices, 8192 vertices for bottom-up, 8192 log entries for the
+// final status reset) that any CTA may claim.  Rows longer than 8192 entries
+// found inside a tile become extra "row jobs", so a hub vertex is spread over
+// many CTAs.  The owner claims tiles of its own step first, then claims tiles
+// of other slots while it waits for its step to complete; CTAs without queries
+// left only claim tiles.
+//
+// Claiming: slot.next packs {seq:20, ntiles:22, next tile:22} in one 64-bit
+// word.  The owner publishes a step by writing its description and then
+// storing a new seq (release).  A helper claims tile i of step seq with a CAS
+// on the whole word, so a claim can never land on a newer step; the owner
+// itself claims with atomicAdd.  A row job adds one to ntiles with an atomic
+// add on the same word after writing its descriptor; a helper that claims a
+// job waits (bounded) for the descriptor's seq stamp.  The step is complete
+// when `done` (read first) equals ntiles (read second).
+//
+// All CTAs of the launch are co-resident (cooperative launch), so waiting on
+// another CTA's progress is safe; every wait is still bounded by %globaltimer
+// and reports FC_ERR_TIMEOUT through ctr[3] instead of hanging.
+#include <climits>
+#include <cstring>
+
+#include "fc_pool.h"
+#include "fc_sched.cuh"
+
+namespace fc {
+
+constexpr int POOL_TILE_V = 8192;    // vertices per bottom-up tile
+constexpr int POOL_TILE_R = 8192;    // log entries per reset tile
+constexpr int POOL_SPLIT_E = 8192;   // row-job length
+constexpr int POOL_JOBS = 4096;      // row jobs per slot and step
+constexpr unsigned long long PK_MASK = (1ull << 22) - 1;
+constexpr unsigned long long POOL_IDLE_NS = 4000000000ull;  // 4 s without progress
+
+enum { DIR_RESET = 2 };
+enum { CTR_NEXT = 0, CTR_FINISHED = 1, CTR_SPILL = 2, CTR_ERR = 3, CTR_INVALID = 4 };
+
+__host__ __device__ inline unsigned long long pk(unsigned seq, unsigned long long ntiles,
+                                                 unsigned long long tile)
+{
+    return ((unsigned long long)(seq & 0xFFFFFu) << 44) | (ntiles << 22) | tile;
+}
+__device__ __forceinline__ unsigned pk_seq(unsigned long long v) { return (unsigned)(v >> 44); }
+__device__ __forceinline__ int pk_ntiles(unsigned long long v) { return (int)((v >> 22) & PK_MASK); }
+__device__ __forceinline__ int pk_tile(unsigned long long v) { return (int)(v & PK_MASK); }
+
+struct RowJob {
+    int b, e;
+    unsigned seq;
+    int pad;
+};
+
+// Step description: written by the owner before it publishes the step.
+struct PoolDesc {
+    int q, gidx, mode, side, dir, level, other_radius, F, front_off, nvt, cap, nreset;
+    uint8_t *status;
+    int32_t *levels;
+    int32_t *log;
+};
+
+struct alignas(256) PoolSlot {
+    unsigned long long next;
+    int done;
+    int njobs;
+    PoolDesc d;
+    TeamCounters tc;
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Row jobs of one published step.
+struct SlotSink {
+    PoolSlot *slot;
+    RowJob *jobs;
+    unsigned seq;
+    __device__ bool push_row(int b, int e) const
+    {
+        if (e - b <= POOL_SPLIT_E) return false;
+        int n = (e - b + POOL_SPLIT_E - 1) / POOL_SPLIT_E;
+        int k = atomicAdd(&slot->njobs, n);
+        if (k + n > POOL_JOBS) return false;  // job space exhausted: walk in place
+        for (int i = 0; i < n; ++i) {
+            RowJob &J = jobs[k + i];
+            J.b = b + i * POOL_SPLIT_E;
+            J.e = min(e, J.b + POOL_SPLIT_E);
+            __threadfence();
+            *(volatile unsigned *)&J.seq = seq;
+        }
+        __threadfence();
+        atomicAdd(&slot->next, (unsigned long long)n << 22);
+        return true;
+    }
+};
+
+template <int T>
+struct SmemPool {
+    SmemTopDown<T> td;
+    QLocal ql;
+    PoolDesc d;  // description of the step whose tile this CTA is running
+    int q, li, publish, flag, cand, claimed, cursor;
+    unsigned seq, my_seq;
+    int err;
+    unsigned long long t_idle;
+};
+
+// ---------------------------------------------------------------------------
+// One tile of a published step (any CTA).  sm.d holds the step description.
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ void pool_tile(const PoolArgs &a, PoolSlot *slot, int tile, unsigned seq,
+                          SmemPool<T> &sm)
+{
+    const PoolDesc &d = sm.d;
+    const int tid = threadIdx.x;
+    if (d.dir == DIR_RESET) {
+        const int n0 = d.F;  // entries of side 0; the rest belong to side 1
+        const int lo = tile * POOL_TILE_R, hi = min(d.nreset, lo + POOL_TILE_R);
+        for (int i = lo + tid; i < hi; i += T) {
+            int v = i < n0 ? d.log[i] : d.log[d.cap - 1 - (i - n0)];
+            d.status[v] = ST_UNVISITED;
+        }
+        return;
+    }
+    if (d.mode == MODE_STCON && ld_cg(&slot->tc.found)) return;  // already met
+    const GraphPair &gp = a.graphs[d.gidx];
+    const DGraph &gx = d.side ? gp.rev : gp.fwd;
+    AppendTarget app{d.log, d.cap, d.side, &slot->tc.tail[d.side], &slot->tc.deg[d.side],
+                     gx.row_ptr};
+    if (tile >= d.nvt) {
+        // row job: wait (bounded) until its descriptor carries this step's seq
+        RowJob *J = a.jobs + (size_t)(slot - a.slots) * POOL_JOBS + (tile - d.nvt);
+        __shared__ int jb, je;
+        if (tid == 0) {
+            unsigned long long t0 = global_timer_ns();
+            jb = je = 0;
+            while (true) {
+                if (*(volatile unsigned *)&J->seq == seq) {
+                    jb = *(volatile int *)&J->b;
+                    je = *(volatile int *)&J->e;
+                    break;
+                }
+                if (global_timer_ns() - t0 > BARRIER_TIMEOUT_NS) {
+                    atomicCAS(&a.ctr[CTR_ERR], 0, FC_ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __syncthreads();
+        const int b = jb, e = je;
+        __syncthreads();
+        if (d.mode == MODE_BFS) {
+            VisitBFS vis{d.levels, d.level + 1};
+            walk_range(gx.col, b, e, tid, T, vis, app);
+        } else {
+            VisitSTCON vis{d.status, st_code(d.side, d.level + 1), d.side, &slot->tc.found};
+            walk_range(gx.col, b, e, tid, T, vis, app);
+        }
+        return;
+    }
+    if (d.dir == DIR_TD) {
+        const int i = tile * T + tid;
+        int rb = 0, re = 0;
+        if (i < d.F) {
+            int u = ld_cg(d.log + d.front_off + i);
+            rb = __ldg(gx.row_ptr + u);
+            re = __ldg(gx.row_ptr + u + 1);
+        }
+        SlotSink sink{slot, a.jobs + (size_t)(slot - a.slots) * POOL_JOBS, seq};
+        if (d.mode == MODE_BFS) {
+            VisitBFS vis{d.levels, d.level + 1};
+            expand_rows<T>(gx.col, rb, re, vis, app, sm.td, sink);
+        } else {
+            VisitSTCON vis{d.status, st_code(d.side, d.level + 1), d.side, &slot->tc.found};
+            expand_rows<T>(gx.col, rb, re, vis, app, sm.td, sink);
+        }
+        return;
+    }
+    // bottom-up over vertices [tile * TILE_V, ...) of the reverse graph
+    const DGraph &gr = d.side ? gp.fwd : gp.rev;
+    const int nv = gr.nv;
+    const int v0 = tile * POOL_TILE_V, v1 = min(nv, v0 + POOL_TILE_V);
+    int inspected = 0;
+    for (int base = v0; base < v1; base += T) {
+        int v = base + tid;
+        int c[1] = {-1};
+        if (v < v1) {
+            if (d.mode == MODE_BFS) {
+                BottomUpBFS bu{d.levels, d.level};
+                c[0] = bu.check(v, gr.row_ptr, gr.col, inspected);
+            } else {
+                BottomUpSTCON bu{d.status, st_code(d.side, d.level), st_code(d.side, d.level + 1),
+                                 st_code(1 - d.side, d.other_radius), &slot->tc.found};
+                c[0] = bu.check(v, gr.row_ptr, gr.col, inspected);
+            }
+        }
+        warp_append<1>(c, app);
+    }
+    int w = warp_sum_i(inspected);
+    if (lane_id() == 0 && w) atomicAdd(&slot->tc.inspected, (unsigned long long)w);
+}
+
+__device__ __forceinline__ void copy_desc(PoolDesc &dst, const PoolDesc *src)
+{
+    const int *s = reinterpret_cast<const int *>(src);
+    int *d = reinterpret_cast<int *>(&dst);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(PoolDesc) / sizeof(int)); ++i) d[i] = __ldcg(s + i);
+}
+
+// Claim and run one tile of some other open step.  Returns true only when a
+// tile was run (callers treat that as progress).  All threads call.
+template <int T>
+__device__ bool pool_steal(const PoolArgs &a, SmemPool<T> &sm)
+{
+    const int P = gridDim.x, tid = threadIdx.x;
+    if (tid == 0) sm.cand = INT_MAX;
+    __syncthreads();
+    const int cur = sm.cursor;
+    for (int k = tid; k < P; k += T) {
+        int j = (cur + k) % P;
+        unsigned long long v = __ldcg(&a.slots[j].next);
+        if (pk_tile(v) < pk_ntiles(v)) atomicMin(&sm.cand, k);
+    }
+    __syncthreads();
+    if (sm.cand == INT_MAX) return false;
+    const int j = (cur + sm.cand) % P;
+    PoolSlot *slot = a.slots + j;
+    if (tid == 0) {
+        sm.claimed = -1;
+        for (int attempt = 0; attempt < 16; ++attempt) {
+            unsigned long long v = ld_acquire_u64(&slot->next);
+            if (pk_tile(v) >= pk_ntiles(v)) break;
+            if (atomicCAS(&slot->next, v, v + 1) == v) {
+                sm.claimed = pk_tile(v);
+                sm.seq = pk_seq(v);
+                copy_desc(sm.d, &slot->d);
+                break;
+            }
+        }
+        sm.cursor = j;  // stay with this slot while it has work
+    }
+    __syncthreads();
+    const int t = sm.claimed;
+    if (t < 0) return false;  // lost every CAS: no progress made
+    pool_tile<T>(a, slot, t, sm.seq, sm);
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        atomicAdd(&slot->done, 1);
+    }
+    return true;
+}
+
+// Publish a step of my slot, run its tiles, help others until it completes.
+template <int T>
+__device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const PoolDesc &desc,
+                                     int nvt, SmemPool<T> &sm)
+{
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        my->d = desc;
+        my->done = 0;
+        my->njobs = 0;
+        sm.my_seq = (sm.my_seq + 1) & 0xFFFFFu;
+        if (sm.my_seq == 0) sm.my_seq = 1;
+        __threadfence();
+        atomicExch(&my->next, pk(sm.my_seq, (unsigned long long)nvt, 0));
+        sm.d = desc;
+    }
+    __syncthreads();
+    // own tiles
+    while (true) {
+        if (tid == 0) {
+            unsigned long long v = atomicAdd(&my->next, 1ull);
+            sm.claimed = pk_tile(v) < pk_ntiles(v) ? pk_tile(v) : -1;
+        }
+        __syncthreads();
+        const int t = sm.claimed;
+        if (t < 0) break;
+        pool_tile<T>(a, my, t, sm.my_seq, sm);
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            atomicAdd(&my->done, 1);
+            sm.d = desc;  // a helper run may not have replaced it, but keep it exact
+        }
+        __syncthreads();
+    }
+    // wait for helpers, helping others meanwhile
+    if (tid == 0) sm.t_idle = global_timer_ns();
+    while (true) {
+        if (tid == 0) {
+            int dn = ld_acquire_gpu(&my->done);
+            unsigned long long v = ld_acquire_u64(&my->next);
+            sm.flag = dn >= pk_ntiles(v) ? 1 : 0;
+            if (!sm.flag && global_timer_ns() - sm.t_idle > POOL_IDLE_NS) {
+                atomicCAS(&a.ctr[CTR_ERR], 0, FC_ERR_TIMEOUT);
+                sm.flag = 2;
+            }
+            if (!sm.flag && ld_cg(&a.ctr[CTR_ERR])) sm.flag = 2;
+        }
+        __syncthreads();
+        if (sm.flag) break;
+        if (pool_steal<T>(a, sm)) {
+            if (tid == 0) sm.t_idle = global_timer_ns();
+        } else if (tid == 0) {
+            __nanosleep(128);
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        sm.err = sm.flag == 2;
+        sm.d = desc;
+    }
+    __syncthreads();
+}
+
+// Run query q with my slot as owner.
+template <int T>
+__device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *status, int32_t *log,
+                           SmemPool<T> &sm)
+{
+    const int tid = threadIdx.x;
+    const int gidx = a.graph_idx ? a.graph_idx[q] : 0;
+    const GraphPair gp = a.graphs[gidx];
+    const int nv = gp.fwd.nv;
+    const int s = a.qs[q];
+    const int t = a.mode == MODE_STCON ? a.qt[q] : s;
+    const int cap = a.exclusive ? nv : min(nv, a.log_cap);
+    if (s < 0 || s >= nv || t < 0 || t >= nv) {
+        if (tid == 0) {
+            if (a.out_conn) a.out_conn[q] = 0;
+            if (a.out_hops) a.out_hops[q] = -2;
+            atomicExch(&a.ctr[CTR_INVALID], 1);
+            __threadfence();
+            atomicAdd(&a.ctr[CTR_FINISHED], 1);
+        }
+        __syncthreads();
+        return;
+    }
+    int32_t *levels = a.levels;
+    if (tid == 0) {
+        init_roots(a.mode, gp, s, t, status, levels, log, cap, &my->tc);
+        __threadfence();
+        ql_start(sm.ql, a.mode == MODE_STCON, nv, gp.fwd.ne, s, t, my->tc.deg[0], my->tc.deg[1]);
+        sm.err = 0;
+    }
+    __syncthreads();
+    PoolDesc desc;
+    desc.q = q;
+    desc.gidx = gidx;
+    desc.mode = a.mode;
+    desc.cap = cap;
+    desc.status = status;
+    desc.levels = levels;
+    desc.log = log;
+    desc.nreset = 0;
+    while (true) {
+        if (tid == 0 && !sm.ql.done) {
+            ql_decide(sm.ql, a.sched, 1, a.mode == MODE_BFS ? INT_MAX : LEVEL7_MAX);
+            const int x = sm.ql.side;
+            const long long m = (long long)(sm.ql.dt[x] - sm.ql.dh[x]);
+            if (!a.exclusive && (long long)sm.ql.tail[0] + sm.ql.tail[1] + m > cap) {
+                sm.ql.escalate = 1;  // the log could overflow: finish it in exclusive mode
+                sm.ql.done = 1;
+            }
+            sm.publish = sm.ql.dir == DIR_BU || m > a.private_edges;
+        }
+        __syncthreads();
+        if (sm.ql.done) break;
+        const int x = sm.ql.side;
+        int F;
+        const int32_t *front = ql_frontier(sm.ql, log, cap, x, &F);
+        if (!sm.publish) {
+            run_step<T>(a.mode, gp, x, DIR_TD, sm.ql.radius[x], sm.ql.radius[1 - x], front, F, 0, 1,
+                        status, levels, log, cap, &my->tc.tail[x], &my->tc.deg[x], &my->tc.found,
+                        &my->tc.inspected, sm.td);
+            __syncthreads();
+        } else {
+            desc.side = x;
+            desc.dir = sm.ql.dir;
+            desc.level = sm.ql.radius[x];
+            desc.other_radius = sm.ql.radius[1 - x];
+            desc.F = F;
+            desc.front_off = (int)(front - log);
+            const int nvt = desc.dir == DIR_TD ? (F + T - 1) / T : (nv + POOL_TILE_V - 1) / POOL_TILE_V;
+            desc.nvt = nvt;
+            pool_publish_and_run<T>(a, my, desc, nvt, sm);
+            if (sm.err) return;
+        }
+        if (tid == 0)
+            ql_update(sm.ql, ld_cg(&my->tc.found), ld_cg(&my->tc.tail[x]), ld_cg_u64(&my->tc.deg[x]),
+                      ld_cg_u64(&my->tc.inspected));
+        __syncthreads();
+    }
+    if (tid == 0) {
+        if (sm.ql.escalate) {
+            int k = atomicAdd(&a.ctr[CTR_SPILL], 1);
+            a.spill[k] = q;
+        }
+        write_result(q, sm.ql, a.out_conn, a.out_hops, a.qstat, sm.ql.escalate);
+    }
+    // clear exactly the claimed status bytes (s-t mode), sharing big resets
+    if (a.mode == MODE_STCON) {
+        const int n0 = sm.ql.tail[0], n1 = sm.ql.tail[1];
+        if (n0 + n1 <= 4 * POOL_TILE_R) {
+            for (int i = tid; i < n0 + n1; i += T) {
+                int v = i < n0 ? log[i] : log[cap - 1 - (i - n0)];
+                status[v] = ST_UNVISITED;
+            }
+        } else {
+            desc.F = n0;
+            desc.dir = DIR_RESET;
+            desc.nreset = n0 + n1;
+            desc.nvt = (n0 + n1 + POOL_TILE_R - 1) / POOL_TILE_R;
+            pool_publish_and_run<T>(a, my, desc, desc.nvt, sm);
+            if (sm.err) return;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        atomicAdd(&a.ctr[CTR_FINISHED], 1);
+    }
+    __syncthreads();
+}
+
+template <int T>
+__global__ void __launch_bounds__(T) k_pool(PoolArgs a)
+{
+    __shared__ SmemPool<T> sm;
+    const int tid = threadIdx.x;
+    PoolSlot *my = a.slots + blockIdx.x;
+    const int nq = a.list_count ? ld_cg(a.list_count) : a.nlist;
+    if (tid == 0) {
+        sm.cursor = (int)((blockIdx.x * 97u) % gridDim.x);
+        sm.li = 0;
+        sm.err = 0;
+        // continue this slot's seq numbering across launches
+        sm.my_seq = pk_seq(__ldcg(&my->next));
+    }
+    __syncthreads();
+    if (!a.exclusive || blockIdx.x == 0) {
+        uint8_t *status = a.status_base + (a.exclusive ? 0 : (size_t)blockIdx.x * a.status_stride);
+        int32_t *log = a.log_base + (a.exclusive ? 0 : (size_t)blockIdx.x * a.log_stride);
+        while (true) {
+            if (tid == 0) sm.q = a.exclusive ? sm.li++ : atomicAdd(&a.ctr[CTR_NEXT], 1);
+            __syncthreads();
+            const int qi = sm.q;
+            if (qi >= nq || ld_cg(&a.ctr[CTR_ERR])) break;
+            pool_query<T>(a, my, a.list ? a.list[qi] : qi, status, log, sm);
+            if (sm.err) break;
+        }
+    }
+    // help until every query is finished
+    if (tid == 0) sm.t_idle = global_timer_ns();
+    __syncthreads();
+    while (true) {
+        if (tid == 0) {
+            sm.flag = ld_acquire_gpu(&a.ctr[CTR_FINISHED]) >= nq || ld_cg(&a.ctr[CTR_ERR]) != 0;
+            if (!sm.flag && global_timer_ns() - sm.t_idle > POOL_IDLE_NS) {
+                atomicCAS(&a.ctr[CTR_ERR], 0, FC_ERR_TIMEOUT);
+                sm.flag = 1;
+            }
+        }
+        __syncthreads();
+        if (sm.flag) break;
+        if (pool_steal<T>(a, sm)) {
+            if (tid == 0) sm.t_idle = global_timer_ns();
+        } else if (tid == 0) {
+            __nanosleep(256);
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+size_t pool_slot_bytes() { return sizeof(PoolSlot); }
+size_t pool_job_bytes() { return sizeof(RowJob) * POOL_JOBS; }
+
+int pool_grid(int sm_count, int ctas_per_sm)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pool<FC_BLOCK>, FC_BLOCK, 0) !=
+            cudaSuccess ||
+        per_sm < 1)
+        return 0;
+    if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
+    return per_sm * sm_count;
+}
+
+int pool_launch(const PoolArgs &a, int grid, cudaStream_t st)
+{
+    PoolArgs args = a;
+    void *kargs[] = {&args};
+    FC_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_pool<FC_BLOCK>, dim3(grid),
+                                            dim3(FC_BLOCK), kargs, 0, st));
+    return FC_OK;
+}
+
+}  // namespace fc

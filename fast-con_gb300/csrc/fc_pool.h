@@ -1,0 +1,46 @@
+// fc_pool.h -- host interface of the work-sharing engine (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fc_engine.h"
+
+namespace fc {
+
+struct GraphPair;
+struct PoolSlot;
+struct RowJob;
+
+struct PoolArgs {
+    const GraphPair *graphs;
+    const int32_t *graph_idx;
+    const int32_t *qs;
+    const int32_t *qt;
+    const int32_t *list;      // optional subset of query indices
+    const int *list_count;    // device count of list entries (nullable)
+    int nlist;                // count when list_count is NULL
+    int mode, sched;
+    int exclusive;            // 1: CTA 0 owns every query in turn, arrays span the graph
+    PoolSlot *slots;          // one per CTA
+    RowJob *jobs;             // POOL_JOBS per CTA
+    uint8_t *status_base;
+    size_t status_stride;
+    int32_t *levels;          // BFS mode (exclusive only)
+    int32_t *log_base;
+    size_t log_stride;
+    int log_cap;
+    long long private_edges;  // steps reading more entries than this are shared
+    int *ctr;                 // [0] next query [1] finished [2] spill count [3] error [4] invalid
+    int32_t *spill;
+    int32_t *out_conn;
+    int32_t *out_hops;
+    QueryStat *qstat;
+};
+
+size_t pool_slot_bytes();
+size_t pool_job_bytes();  // per slot
+int pool_grid(int sm_count, int ctas_per_sm);
+int pool_launch(const PoolArgs &a, int grid, cudaStream_t st);
+
+}  // namespace fc

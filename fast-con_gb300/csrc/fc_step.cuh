@@ -165,6 +165,73 @@ __device__ __forceinline__ int block_inclusive_scan(int x, int *warp_tot, int *t
     return r;
 }
 
+// Hook for rows too long for one CTA: a published (shared) step hands them
+// out as row jobs; everywhere else rows are walked in place.
+struct NoSink {
+    __device__ __forceinline__ bool push_row(int, int) const { return false; }
+};
+
+// ---------------------------------------------------------------------------
+// Expand one tile of frontier vertices; thread tid holds the row [rb, re) of
+// its vertex (empty when it has none).  All threads of the CTA call it.
+// ---------------------------------------------------------------------------
+template <int T, class Vis, class Sink>
+__device__ __forceinline__ void expand_rows(const int32_t *__restrict__ col, int rb, int re,
+                                            const Vis &vis, const AppendTarget &app,
+                                            SmemTopDown<T> &sm, const Sink &sink)
+{
+    const int tid = threadIdx.x, lane = tid & 31;
+    // class 1: rows of >= T entries, whole CTA (or row jobs for very long rows)
+    while (true) {
+        if (tid == 0) sm.owner = -1;
+        __syncthreads();
+        if (re - rb >= T) sm.owner = tid;
+        __syncthreads();
+        int w = sm.owner;
+        if (w < 0) break;
+        if (tid == w) {
+            if (sink.push_row(rb, re)) {
+                sm.rb = sm.re = 0;
+            } else {
+                sm.rb = rb;
+                sm.re = re;
+            }
+            rb = re;
+        }
+        __syncthreads();
+        walk_range(col, sm.rb, sm.re, tid, T, vis, app);
+    }
+    // class 2: rows of >= 32 entries, one warp
+    while (true) {
+        unsigned m = __ballot_sync(0xffffffffu, re - rb >= 32);
+        if (!m) break;
+        int leader = __ffs(m) - 1;
+        int b = __shfl_sync(0xffffffffu, rb, leader);
+        int e = __shfl_sync(0xffffffffu, re, leader);
+        if (lane == leader) rb = re;
+        walk_range(col, b, e, lane, 32, vis, app);
+    }
+    // class 3: short rows, CTA scan + shared-memory gather
+    int d = re - rb;
+    int incl = block_inclusive_scan<T>(d, sm.warp_tot, &sm.total);
+    int off = incl - d;
+    const int total = sm.total;
+    constexpr int G = T * GATHER_PER_THREAD;
+    for (int chunk = 0; chunk < total; chunk += G) {
+        int lo = max(off, chunk), hi = min(off + d, chunk + G);
+        for (int j = lo; j < hi; ++j) sm.gather[j - chunk] = rb + (j - off);
+        __syncthreads();
+        int cnt = min(G, total - chunk);
+        for (int k0 = 0; k0 < cnt; k0 += T) {
+            int k = k0 + tid;
+            int c[1] = {-1};
+            if (k < cnt) c[0] = vis.visit(__ldg(col + sm.gather[k]));
+            warp_append<1>(c, app);
+        }
+        __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Top-down step over frontier[0, F).  Tiles of T frontier vertices are dealt
 // round-robin to the team's CTAs.  `stop_flag` (nullable) is polled once per
@@ -176,7 +243,7 @@ __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t 
                              const Vis &vis, const AppendTarget &app, SmemTopDown<T> &sm,
                              const int *stop_flag)
 {
-    const int tid = threadIdx.x, lane = tid & 31;
+    const int tid = threadIdx.x;
     for (long long base = (long long)team_rank * T; base < F; base += (long long)team_size * T) {
         int i = (int)base + tid;
         int rb = 0, re = 0;
@@ -185,51 +252,7 @@ __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t 
             rb = __ldg(row_ptr + u);
             re = __ldg(row_ptr + u + 1);
         }
-        // class 1: rows of >= T entries, whole CTA
-        while (true) {
-            if (tid == 0) sm.owner = -1;
-            __syncthreads();
-            if (re - rb >= T) sm.owner = tid;
-            __syncthreads();
-            int w = sm.owner;
-            if (w < 0) break;
-            if (tid == w) {
-                sm.rb = rb;
-                sm.re = re;
-                rb = re;
-            }
-            __syncthreads();
-            walk_range(col, sm.rb, sm.re, tid, T, vis, app);
-        }
-        // class 2: rows of >= 32 entries, one warp
-        while (true) {
-            unsigned m = __ballot_sync(0xffffffffu, re - rb >= 32);
-            if (!m) break;
-            int leader = __ffs(m) - 1;
-            int b = __shfl_sync(0xffffffffu, rb, leader);
-            int e = __shfl_sync(0xffffffffu, re, leader);
-            if (lane == leader) rb = re;
-            walk_range(col, b, e, lane, 32, vis, app);
-        }
-        // class 3: short rows, CTA scan + shared-memory gather
-        int d = re - rb;
-        int incl = block_inclusive_scan<T>(d, sm.warp_tot, &sm.total);
-        int off = incl - d;
-        const int total = sm.total;
-        constexpr int G = T * GATHER_PER_THREAD;
-        for (int chunk = 0; chunk < total; chunk += G) {
-            int lo = max(off, chunk), hi = min(off + d, chunk + G);
-            for (int j = lo; j < hi; ++j) sm.gather[j - chunk] = rb + (j - off);
-            __syncthreads();
-            int cnt = min(G, total - chunk);
-            for (int k0 = 0; k0 < cnt; k0 += T) {
-                int k = k0 + tid;
-                int c[1] = {-1};
-                if (k < cnt) c[0] = vis.visit(__ldg(col + sm.gather[k]));
-                warp_append<1>(c, app);
-            }
-            __syncthreads();
-        }
+        expand_rows<T>(col, rb, re, vis, app, sm, NoSink{});
         if (stop_flag) {
             if (tid == 0) sm.stop = *(volatile const int *)stop_flag;
             __syncthreads();

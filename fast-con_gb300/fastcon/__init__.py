@@ -51,7 +51,7 @@ class Opts(ctypes.Structure):
     _fields_ = [("sched", ctypes.c_int32), ("engine", ctypes.c_int32), ("block", ctypes.c_int32),
                 ("ctas_per_sm", ctypes.c_int32), ("use_graph", ctypes.c_int32),
                 ("max_slots", ctypes.c_int32), ("stream", ctypes.c_void_p),
-                ("reserved", ctypes.c_int32 * 8)]
+                ("cta_work_k", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
 
 
 class Stats(ctypes.Structure):
@@ -131,12 +131,13 @@ def _i32(a):
 
 
 def make_opts(sched=SCHED_HEURISTIC, engine=ENGINE_AUTO, block=0, ctas_per_sm=0, use_graph=0,
-              max_slots=0, stream=None) -> Opts:
+              max_slots=0, stream=None, cta_work_k=0) -> Opts:
     o = Opts()
     lib().fc_opts_init(ctypes.byref(o))
     o.sched, o.engine, o.block, o.ctas_per_sm = sched, engine, block, ctas_per_sm
     o.use_graph, o.max_slots = use_graph, max_slots
     o.stream = stream
+    o.cta_work_k = cta_work_k
     return o
 
 

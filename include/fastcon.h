@@ -64,8 +64,13 @@ typedef struct fc_opts {
     int32_t ctas_per_sm;  /* resident CTAs per SM for batched (0 = tuned)   */
     int32_t use_graph;    /* batched: capture the launch in a CUDA graph    */
     int32_t max_slots;    /* batched: cap on concurrent queries (0 = all)   */
-    void   *stream;       /* cudaStream_t, NULL = the handle's own stream   */
-    int32_t reserved[8];
+    void   *stream;       /* cudaStream_t, NULL = the library's own stream  */
+    int32_t cta_work_k;   /* work-sharing engine: a step reading more than
+                             cta_work_k * 1024 adjacency entries is cut into
+                             tiles that every CTA may take (0 = 16 for
+                             batches, 4 for single queries; < 0 = share
+                             every step)                                    */
+    int32_t reserved[7];
 } fc_opts;
 
 typedef struct fc_stats {

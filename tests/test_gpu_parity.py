@@ -11,7 +11,7 @@ from fastcon import graphs
 
 pytestmark = pytest.mark.gpu
 
-ENGINES_SINGLE = ["hostloop", "persistent"]
+ENGINES_SINGLE = ["hostloop", "persistent", "batched"]
 ENGINES_BATCH = ["batched", "persistent", "hostloop"]
 SCHEDS = ["plain", "heuristic", "learned"]
 
@@ -98,7 +98,8 @@ def test_er_device_ingest_is_canonical(er_graph, er_golden):
 
 
 @pytest.mark.parametrize("engine,sched", [("hostloop", "plain"), ("persistent", "plain"),
-                                          ("persistent", "heuristic"), ("hostloop", "heuristic")])
+                                          ("persistent", "heuristic"), ("hostloop", "heuristic"),
+                                          ("batched", "plain"), ("batched", "heuristic")])
 def test_er_bfs_levels_match_reference(fastcon_lib, er_graph, er_golden, engine, sched):
     o = opts(fastcon_lib, engine, sched)
     bu = 0
@@ -297,3 +298,35 @@ def test_batched_many_queries_rmat(fastcon_lib, oracle_mod):
             conn, hops, st = fc.stcon_batch(G, s, t, opts=opts(fc, eng, sch), stats=True)
             assert (hops == want).all(), (eng, sch)
             assert st["edges_inspected"] > 0
+
+
+# --------------------------------------------------------------------------
+# the work-sharing engine with every step shared: tiles, row jobs for hub
+# rows longer than 8,192 entries, shared status resets
+# --------------------------------------------------------------------------
+def test_shared_steps_and_row_jobs(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    rng = np.random.default_rng(8)
+    nv = 70000
+    # two hubs of 30,000 and 12,000 leaves, a long path, random extra edges
+    u = np.concatenate([np.zeros(30000), np.full(12000, 1), np.arange(50000, 69999),
+                        rng.integers(0, nv, 20000)]).astype(np.int32)
+    v = np.concatenate([np.arange(2, 30002), np.arange(30002, 42002), np.arange(50001, 70000),
+                        rng.integers(0, nv, 20000)]).astype(np.int32)
+    G = fc.Graph.from_edges(u, v, nv)
+    rp, col = oracle_mod.build_csr(nv, u, v)
+    s, t = graphs.uniform_pairs(nv, 300, seed=21)
+    s[:4] = [0, 1, 50000, 0]
+    t[:4] = [1, 69999, 2, 60000]
+    _, want, _ = oracle_mod.stcon_batch(rp, col, s, t, nthreads=4)
+    for work_k in (-1, 1, 0):
+        for sch in SCHEDS:
+            o = fc.make_opts(sched={"plain": 0, "heuristic": 1, "learned": 2}[sch],
+                             engine=fc.ENGINE_BATCHED, cta_work_k=work_k)
+            conn, hops = fc.stcon_batch(G, s, t, opts=o)
+            assert (hops == want).all(), (work_k, sch)
+            for k in range(0, 300, 37):
+                assert G.stcon(s[k], t[k], o) == (want[k] >= 0, want[k])
+            for src in (0, 1, 50000, 7):
+                lev, _ = oracle_mod.bfs_levels(rp, col, src)
+                assert (G.bfs_levels(src, o) == lev).all(), (work_k, sch, src)
