@@ -135,7 +135,11 @@ __device__ void pool_tile(const PoolArgs &a, PoolSlot *slot, int tile, unsigned 
         }
         return;
     }
-    if (d.mode == MODE_STCON && ld_cg(&slot->tc.found)) return;  // already met
+    // already met: skip the tile (one read, shared, so the whole CTA agrees)
+    __shared__ int s_met;
+    if (tid == 0) s_met = d.mode == MODE_STCON && ld_cg(&slot->tc.found);
+    __syncthreads();
+    if (s_met) return;
     const GraphPair &gp = a.graphs[d.gidx];
     const DGraph &gx = d.side ? gp.rev : gp.fwd;
     AppendTarget app{d.log, d.cap, d.side, &slot->tc.tail[d.side], &slot->tc.deg[d.side],
@@ -283,11 +287,20 @@ __device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const Pool
         sm.d = desc;
     }
     __syncthreads();
-    // own tiles
+    // own tiles (claimed by CAS like everyone else: the tile counter never
+    // runs past ntiles, so indices that row jobs add later stay claimable)
     while (true) {
         if (tid == 0) {
-            unsigned long long v = atomicAdd(&my->next, 1ull);
-            sm.claimed = pk_tile(v) < pk_ntiles(v) ? pk_tile(v) : -1;
+            sm.claimed = -1;
+            unsigned long long v = ld_acquire_u64(&my->next);
+            while (pk_tile(v) < pk_ntiles(v)) {
+                unsigned long long w = atomicCAS(&my->next, v, v + 1);
+                if (w == v) {
+                    sm.claimed = pk_tile(v);
+                    break;
+                }
+                v = w;
+            }
         }
         __syncthreads();
         const int t = sm.claimed;
@@ -459,10 +472,13 @@ __global__ void __launch_bounds__(T) k_pool(PoolArgs a)
         uint8_t *status = a.status_base + (a.exclusive ? 0 : (size_t)blockIdx.x * a.status_stride);
         int32_t *log = a.log_base + (a.exclusive ? 0 : (size_t)blockIdx.x * a.log_stride);
         while (true) {
-            if (tid == 0) sm.q = a.exclusive ? sm.li++ : atomicAdd(&a.ctr[CTR_NEXT], 1);
+            if (tid == 0) {
+                sm.q = a.exclusive ? sm.li++ : atomicAdd(&a.ctr[CTR_NEXT], 1);
+                if (ld_cg(&a.ctr[CTR_ERR])) sm.q = INT_MAX;
+            }
             __syncthreads();
             const int qi = sm.q;
-            if (qi >= nq || ld_cg(&a.ctr[CTR_ERR])) break;
+            if (qi >= nq) break;
             pool_query<T>(a, my, a.list ? a.list[qi] : qi, status, log, sm);
             if (sm.err) break;
         }
