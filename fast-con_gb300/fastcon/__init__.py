@@ -37,6 +37,7 @@ EXPORTS = [
     "fc_graph_from_device_edges", "fc_graph_generate_rmat", "fc_graph_generate_grid",
     "fc_graph_info", "fc_graph_get_csr", "fc_graph_free", "fc_bfs_levels", "fc_bfs_levels_ex",
     "fc_stcon", "fc_stcon_ex", "fc_stcon_depth", "fc_stcon_batch", "fc_stcon_batch_device",
+    "fc_stcon_batch_noalloc",
     "fc_strerror", "fc_last_error_message", "fc_device_info", "fc_version",
 ]
 
@@ -102,6 +103,8 @@ def lib():
             "fc_stcon_depth": (ctypes.c_int, [_VP, _I32, _I32, _VP]),
             "fc_stcon_batch": (ctypes.c_int, [_VP, _I32, _VP, _VP, _VP, _I32, _VP, _VP, _VP, _VP]),
             "fc_stcon_batch_device": (ctypes.c_int, [_VP, _I32, _VP, _VP, _VP, _I32, _VP, _VP, _VP, _VP]),
+            "fc_stcon_batch_noalloc": (ctypes.c_int, [_VP, _VP, _I32, _I64, _VP, _VP, _VP, _VP,
+                                                      _I32, _VP, _VP, _I32, _VP]),
             "fc_strerror": (ctypes.c_char_p, [ctypes.c_int]),
             "fc_last_error_message": (ctypes.c_char_p, []),
             "fc_device_info": (ctypes.c_int, [_VP, _VP, _VP, _VP]),

@@ -181,6 +181,25 @@ int fc_stcon_batch_device(fc_graph *const *gs, int32_t ngraphs, const int32_t *d
                           int32_t *d_connected, int32_t *d_hops, const fc_opts *opts,
                           fc_stats *stats);
 
+/* Batch of s-t queries that allocates nothing (no counterpart in the
+ * reference).  For callers that cannot allocate device memory while they
+ * query -- e.g. a service that reserved all device memory for its own pool
+ * and forbids allocator calls afterwards, or a plug-in inside a framework
+ * that owns the device memory.  The caller passes the graph as device CSR
+ * arrays (d_rrow_ptr / d_rcol: reverse CSR of a directed graph, or NULL for
+ * a symmetric one) and device arrays for queries and results; sched is an
+ * FC_SCHED_* value.  Working memory is a fixed 20 MiB device array inside the
+ * library (held on every GPU that loads it until exit), so graphs are limited
+ * to 1,048,576 vertices (larger: FC_ERR_INVALID).  Calls share that array:
+ * calls whose kernels overlap on the GPU race and must be serialised.  The
+ * first call on a device looks up the array's address (once per device); make
+ * it before any stream capture.  Asynchronous on `stream` (a cudaStream_t);
+ * out-of-range query ids give connected = 0, hops = -2. */
+int fc_stcon_batch_noalloc(const int32_t *d_row_ptr, const int32_t *d_col, int32_t nv, int64_t ne,
+                           const int32_t *d_rrow_ptr, const int32_t *d_rcol, const int32_t *d_s,
+                           const int32_t *d_t, int32_t nq, int32_t *d_connected, int32_t *d_hops,
+                           int32_t sched, void *stream);
+
 /* ---- misc ---------------------------------------------------------------- */
 const char *fc_strerror(int code);
 const char *fc_last_error_message(void);  /* thread-local detail of the last error */
