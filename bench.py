@@ -1,21 +1,23 @@
 """Benchmark: batched s-t connectivity on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fastcon|reference]
-                    [--config rmat24|er65536|grid4096|batched512]
+                    [--config rmat24|rmat22|er65536|grid4096|batched512] [--sched heuristic|plain|learned]
 
 Default workload (rmat24): R-MAT scale 24 (16,777,216 vertices; 8 * 2^24 edge
 samples with a/b/c/d = .57/.19/.19/.05 -> average degree ~16 after
 symmetrisation and deduplication; ids permuted, seed 3), 1,024 (s, t) pairs
-among vertices of degree >= 1 (seed 4).  One step = all 1,024 queries through
-the library's batched engine.  The graph (CSR ~1 GB) is larger than L2, so no
-L2 flush is added between steps.
+among vertices of degree >= 1 (seed 4).  One step = all queries of the
+workload through the library's batched engine.  The rmat24, grid4096 and
+batched512 graphs are larger than L2, so no L2 flush is added between steps.
 
 Printed line (rank 0): value = queries/s with inputs resident in HBM (CUDA
 events on the launching stream); e2e = the same through fc_stcon_batch with
 pinned host arrays (copies inside the timed region); roofline of the
-dominant kernel; cpu_baseline = the reference's CPU path (full BFS per query,
-Graph::bfs semantics) on the host cores; plain = the plain level-synchronous
-GPU form (host-driven, alternating sides, top-down) on a sample.
+dominant kernel (algorithmic bytes per launch / its CUDA-event time); cpu_baseline =
+the reference's CPU path (one full BFS per query, Graph::bfs semantics) on the
+host cores; plain = the plain level-synchronous GPU form (host-driven,
+alternating sides, top-down) on a sample; one_launch_per_query = the library's
+single-query call in a loop on a sample.
 
 --impl reference times the reference's CPU path alone (rank 0) on bounded
 samples of the same workload and prints the same metric with impl=reference.
@@ -48,6 +50,7 @@ CONFIGS = {
     "er65536": dict(kind="er", n=65536, m=524288, seed=1, nq=64, qseed=2),
     "grid4096": dict(kind="grid", w=4096, h=4096, p_del=0.05, del_seed=5, sc_seed=6, nq=256,
                      qseed=7, min_manhattan=2000),
+    "batched512": dict(kind="multi", ngraphs=512, first_seed=100, per_graph=8),
     # smaller R-MAT (same parameters) used for profiler captures
     "rmat22": dict(kind="rmat", scale=22, edge_samples=8 << 22, seed=3, perm_seed=3, nq=1024,
                    qseed=4),
@@ -79,10 +82,11 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            time.sleep(0.3)  # let the sampler start before the timed region
         except (OSError, FileNotFoundError):
             self.proc = None
 
@@ -93,6 +97,7 @@ class ClockSampler:
     def stop(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.15)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -132,50 +137,58 @@ def barrier(ws):
         dist.barrier()
 
 
-def max_over_ranks(ws, x: float) -> float:
+def reduce_over_ranks(ws, x: float, op: str) -> float:
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
     t = torch.tensor([x], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
-
-
-def sum_over_ranks(ws, x: float) -> float:
-    if ws == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
     return float(t.item())
 
 
 # ---------------------------------------------------------------------------
-# workload construction
+# workloads: (graphs, graph index per query or None, s, t)
 # ---------------------------------------------------------------------------
-def make_graph_gpu(fc, cfg):
+def multi_specs(cfg):
+    from fastcon import graphs
+    scales = graphs.batched_scales(cfg["ngraphs"], cfg["first_seed"])
+    return [(cfg["first_seed"] + i, sc) for i, sc in enumerate(scales)]
+
+
+def make_workload_gpu(fc, cfg):
     from fastcon import graphs
     if cfg["kind"] == "rmat":
         G = fc.Graph.rmat(cfg["scale"], cfg["edge_samples"], seed=cfg["seed"],
                           perm_seed=cfg["perm_seed"])
         rp, _ = G.csr_row_ptr()
         s, t = graphs.pairs_with_degree(np.diff(rp), cfg["nq"], seed=cfg["qseed"])
-    elif cfg["kind"] == "er":
+        return [G], None, s, t
+    if cfg["kind"] == "er":
         u, v = graphs.er_edges(cfg["n"], cfg["m"], seed=cfg["seed"])
         G = fc.Graph.from_edges(u, v, cfg["n"])
         s, t = graphs.uniform_pairs(cfg["n"], cfg["nq"], seed=cfg["qseed"])
-    else:
+        return [G], None, s, t
+    if cfg["kind"] == "grid":
         n = cfg["w"] * cfg["h"]
         G = fc.Graph.grid(cfg["w"], cfg["h"], p_del=cfg["p_del"], del_seed=cfg["del_seed"],
                           shortcuts=graphs.grid_shortcut_count(n), sc_seed=cfg["sc_seed"])
         s, t = graphs.grid_pairs(cfg["w"], cfg["h"], cfg["nq"], cfg["qseed"], cfg["min_manhattan"])
-    return G, s, t
+        return [G], None, s, t
+    Gs, ss, ts, gi = [], [], [], []
+    for k, (seed, scale) in enumerate(multi_specs(cfg)):
+        G = fc.Graph.rmat(scale, 8 << scale, seed=seed, perm_seed=seed)
+        rp, _ = G.csr_row_ptr()
+        s, t = graphs.pairs_with_degree(np.diff(rp), cfg["per_graph"], seed=seed)
+        Gs.append(G)
+        ss.append(s)
+        ts.append(t)
+        gi.append(np.full(len(s), k, np.int32))
+    return Gs, np.concatenate(gi), np.concatenate(ss), np.concatenate(ts)
 
 
-def make_graph_cpu(cfg, nthreads):
-    """Host CSR for the CPU arm, built without any GPU code (oracle C)."""
+def make_workload_cpu(cfg, nthreads, only_graphs=None):
+    """Host CSRs for the CPU arm, built without any GPU code (oracle C)."""
     import oracle
     from fastcon import graphs
     if cfg["kind"] == "rmat":
@@ -185,97 +198,128 @@ def make_graph_cpu(cfg, nthreads):
         rp, col = oracle.build_csr(n, u, v, nthreads=nthreads)
         del u, v
         s, t = graphs.pairs_with_degree(np.diff(rp), cfg["nq"], seed=cfg["qseed"])
-    elif cfg["kind"] == "er":
+        return [(rp, col)], None, s, t
+    if cfg["kind"] == "er":
         u, v = graphs.er_edges(cfg["n"], cfg["m"], seed=cfg["seed"])
         rp, col = oracle.build_csr(cfg["n"], u, v, nthreads=nthreads)
         s, t = graphs.uniform_pairs(cfg["n"], cfg["nq"], seed=cfg["qseed"])
-    else:
+        return [(rp, col)], None, s, t
+    if cfg["kind"] == "grid":
         n = cfg["w"] * cfg["h"]
         u, v = graphs.grid_edges(cfg["w"], cfg["h"], cfg["p_del"], cfg["del_seed"],
                                  graphs.grid_shortcut_count(n), cfg["sc_seed"])
         rp, col = oracle.build_csr(n, u, v, nthreads=nthreads)
         s, t = graphs.grid_pairs(cfg["w"], cfg["h"], cfg["nq"], cfg["qseed"], cfg["min_manhattan"])
-    return rp, col, s, t
+        return [(rp, col)], None, s, t
+    csrs, ss, ts, gi = [], [], [], []
+    for k, (seed, scale) in enumerate(multi_specs(cfg)):
+        if only_graphs is not None and k not in only_graphs:
+            csrs.append(None)
+            continue
+        u, v = oracle.gen_rmat(scale, 8 << scale, seed=seed, perm_seed=seed, nthreads=nthreads)
+        rp, col = oracle.build_csr(1 << scale, u, v, nthreads=nthreads)
+        s, t = graphs.pairs_with_degree(np.diff(rp), cfg["per_graph"], seed=seed)
+        csrs.append((rp, col))
+        ss.append(s)
+        ts.append(t)
+        gi.append(np.full(len(s), k, np.int32))
+    return csrs, np.concatenate(gi), np.concatenate(ss), np.concatenate(ts)
 
 
-def cpu_sample_size(cfg):
-    return {"rmat": 32, "er": 64, "grid": 32}[cfg["kind"]]
-
-
-def time_cpu_reference(rp, col, s, t, nthreads, min_seconds=10.0, max_queries=None):
-    """The reference's CPU path (one full BFS per query, Graph::bfs) on a
-    bounded sample; returns (queries/s, queries timed, seconds)."""
+def cpu_queries(csrs, gi, s, t, idx, nthreads):
+    """Run queries idx with the reference's CPU path (full BFS per query)."""
     import oracle
+    hops = np.zeros(len(idx), np.int32)
+    if gi is None:
+        rp, col = csrs[0]
+        _, h, _ = oracle.stcon_batch(rp, col, s[idx], t[idx], nthreads=nthreads)
+        return h
+    for g in np.unique(gi[idx]):
+        m = gi[idx] == g
+        rp, col = csrs[g]
+        _, h, _ = oracle.stcon_batch(rp, col, s[idx][m], t[idx][m], nthreads=nthreads)
+        hops[m] = h
+    return hops
+
+
+def cpu_rate(csrs, gi, s, t, nthreads, min_seconds=10.0, max_queries=None, order=None):
     nq = len(s)
+    order = np.arange(nq) if order is None else order
     done = 0
     t0 = time.perf_counter()
-    chunk = max(nthreads, 1)
     while True:
-        lo = done % nq
-        hi = min(nq, lo + chunk)
-        oracle.stcon_batch(rp, col, s[lo:hi], t[lo:hi], nthreads=nthreads)
-        done += hi - lo
+        idx = order[np.arange(done, done + nthreads) % len(order)]
+        cpu_queries(csrs, gi, s, t, idx, nthreads)
+        done += len(idx)
         el = time.perf_counter() - t0
         if el >= min_seconds or (max_queries and done >= max_queries):
             break
     return done / el, done, el
 
 
+def config_desc(name, cfg, nq):
+    d = {"workload": name, "queries": nq}
+    if cfg["kind"] == "rmat":
+        d.update({"graph": f"R-MAT scale {cfg['scale']}, {cfg['edge_samples']} edge samples "
+                           "(edge factor 16 counted as average degree), a/b/c/d=.57/.19/.19/.05, "
+                           f"ids permuted (seed {cfg['perm_seed']})",
+                  "query_seed": cfg["qseed"], "l2": "inputs larger than L2 (CSR > 126 MB)"})
+    elif cfg["kind"] == "er":
+        d.update({"graph": f"G(n,m) n={cfg['n']} m={cfg['m']} seed {cfg['seed']}",
+                  "l2": "graph fits in L2 (small config)"})
+    elif cfg["kind"] == "grid":
+        d.update({"graph": f"{cfg['w']}x{cfg['h']} grid, {cfg['p_del']:.0%} edges deleted "
+                           "(seed 5), 0.01% n shortcuts (seed 6)",
+                  "min_manhattan": cfg["min_manhattan"], "l2": "inputs larger than L2"})
+    else:
+        d.update({"graph": f"{cfg['ngraphs']} R-MAT graphs, scale uniform in [12,20], 8*2^scale "
+                           f"samples each, seeds {cfg['first_seed']}..{cfg['first_seed'] + cfg['ngraphs'] - 1}",
+                  "l2": "inputs larger than L2"})
+    return d
+
+
 # ---------------------------------------------------------------------------
-# arms
+# reference arm (CPU only)
 # ---------------------------------------------------------------------------
 def run_reference(args, cfg):
     ws, rank, _ = dist_env()
     if ws > 1 and rank != 0:
         return
     nthreads = os.cpu_count() or 1
-    rp, col, s, t = make_graph_cpu(cfg, nthreads)
-    per_step = max(nthreads, cpu_sample_size(cfg))
-    rates = []
+    only = None
+    if cfg["kind"] == "multi":
+        only = set(range(0, cfg["ngraphs"], 16))  # bounded sample of graphs
+    csrs, gi, s, t = make_workload_cpu(cfg, nthreads, only)
+    per_step = max(nthreads, 32)
+    order = np.arange(len(s)) if gi is None else np.flatnonzero(np.isin(gi, list(only)))
+    el_total, q_total, k = 0.0, 0, 0
     for i in range(args.warmup + args.steps):
-        lo = (i * per_step) % len(s)
-        idx = np.arange(lo, lo + per_step) % len(s)
+        idx = order[np.arange(i * per_step, (i + 1) * per_step) % len(order)]
         t0 = time.perf_counter()
-        import oracle
-        oracle.stcon_batch(rp, col, s[idx], t[idx], nthreads=nthreads)
+        cpu_queries(csrs, gi, s, t, idx, nthreads)
         el = time.perf_counter() - t0
         if i >= args.warmup:
-            rates.append((per_step, el))
-    q = sum(r[0] for r in rates)
-    el = sum(r[1] for r in rates)
-    value = q / el
-    kind = "port"
+            el_total += el
+            q_total += len(idx)
+            k += 1
+    value = q_total / el_total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * el / len(rates),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * el_total / k,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic", "config": config_desc(args.config, cfg),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": kind,
-                         "sample": f"{per_step} of the {len(s)} queries per step, one full BFS "
-                                   f"from s per query (Graph::bfs), {nthreads} threads"},
+        "data": "synthetic", "config": config_desc(args.config, cfg, len(s)),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": f"{per_step} queries of the workload per step, one full BFS "
+                                   f"from s per query (Graph::bfs restated in oracle/fc_oracle.c), "
+                                   f"{nthreads} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def config_desc(name, cfg):
-    d = {"workload": name}
-    if cfg["kind"] == "rmat":
-        d.update({"graph": f"R-MAT scale {cfg['scale']}, {cfg['edge_samples']} edge samples "
-                           "(edge factor 16 counted as average degree), a/b/c/d=.57/.19/.19/.05, "
-                           f"ids permuted (seed {cfg['perm_seed']})",
-                  "queries": cfg["nq"], "query_seed": cfg["qseed"],
-                  "l2": "inputs larger than L2 (CSR > 126 MB)"})
-    elif cfg["kind"] == "er":
-        d.update({"graph": f"G(n,m) n={cfg['n']} m={cfg['m']} seed {cfg['seed']}",
-                  "queries": cfg["nq"], "l2": "graph fits in L2 (small config)"})
-    else:
-        d.update({"graph": f"{cfg['w']}x{cfg['h']} grid, {cfg['p_del']:.0%} edges deleted, "
-                           "0.01% shortcuts", "queries": cfg["nq"],
-                  "l2": "inputs larger than L2"})
-    return d
-
-
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
 def run_fastcon(args, cfg):
     import torch
     ws, rank, local = dist_env()
@@ -284,34 +328,33 @@ def run_fastcon(args, cfg):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     import fastcon as fc
-    import oracle
 
-    G, s, t = make_graph_gpu(fc, cfg)
+    sched = {"heuristic": fc.SCHED_HEURISTIC, "plain": fc.SCHED_PLAIN,
+             "learned": fc.SCHED_LEARNED}[args.sched]
+    if args.sched == "learned":
+        from fastcon import learn
+        learn.load_default_weights()
+    Gs, gi, s, t = make_workload_gpu(fc, cfg)
     nq = len(s)
     # a dedicated stream: the library launches on it and the events record on it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    opt = fc.make_opts(sched=fc.SCHED_HEURISTIC, engine=fc.ENGINE_BATCHED,
-                       stream=stream.cuda_stream)
+    opt = fc.make_opts(sched=sched, engine=fc.ENGINE_BATCHED, stream=stream.cuda_stream)
     d_s = torch.from_numpy(s).cuda()
     d_t = torch.from_numpy(t).cuda()
+    d_g = torch.from_numpy(gi).cuda() if gi is not None else None
     d_c = torch.empty(nq, dtype=torch.int32, device="cuda")
     d_h = torch.empty(nq, dtype=torch.int32, device="cuda")
+    gptr = d_g.data_ptr() if d_g is not None else None
 
-    def step():
-        fc.stcon_batch_device(G, d_s.data_ptr(), d_t.data_ptr(), nq, d_c.data_ptr(),
-                              d_h.data_ptr(), opts=opt)
+    def step(stats=False):
+        return fc.stcon_batch_device(Gs, d_s.data_ptr(), d_t.data_ptr(), nq, d_c.data_ptr(),
+                                     d_h.data_ptr(), graph_idx_ptr=gptr, opts=opt, stats=stats)
 
     for _ in range(max(3, args.warmup)):
         step()
     torch.cuda.synchronize()
-    # correctness of this very workload on a sample (oracle, host cores)
     hops_gpu = d_h.cpu().numpy()
-    nthreads = os.cpu_count() or 1
-    rp, col = G.csr()
-    samp = np.arange(0, nq, max(1, nq // 16))
-    _, want, _ = oracle.stcon_batch(rp, col, s[samp], t[samp], nthreads=nthreads)
-    exact = bool((hops_gpu[samp] == want).all())
 
     clocks = ClockSampler(local)
     barrier(ws)
@@ -324,24 +367,21 @@ def run_fastcon(args, cfg):
         step()
     e1.record(stream)
     torch.cuda.synchronize()
-    barrier(ws)
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    ms = max_over_ranks(ws, ms)
-    total_q = sum_over_ranks(ws, float(nq * args.steps))
+    barrier(ws)
+    ms = reduce_over_ranks(ws, e0.elapsed_time(e1), "max")
+    total_q = reduce_over_ranks(ws, float(nq * args.steps), "sum")
     value = total_q / (ms / 1000.0)
 
-    # per-kernel split and algorithmic bytes (same workload, stats on)
-    kms = np.zeros(2)
-    kbytes = np.zeros(2)
-    ins = 0
-    st = None
+    # per-kernel split and algorithmic bytes (same workload, statistics on)
+    kms, kbytes, ins, esc, launches = np.zeros(2), np.zeros(2), 0, 0, 0
     for _ in range(args.steps):
-        st = fc.stcon_batch_device(G, d_s.data_ptr(), d_t.data_ptr(), nq, d_c.data_ptr(),
-                                   d_h.data_ptr(), opts=opt, stats=True)
+        st = step(stats=True)
         kms += np.array(st["kernel_ms"])
         kbytes += np.array(st["kernel_alg_bytes"])
         ins += st["edges_inspected"]
+        esc = st["escalated"]
+        launches = st["launches"]
     kms /= args.steps
     kbytes /= args.steps
     dom = int(np.argmax(kms))
@@ -349,42 +389,61 @@ def run_fastcon(args, cfg):
     achieved = (kbytes[dom] / 1e9) / (kms[dom] / 1e3) if kms[dom] > 0 else 0.0
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": None,
-                "kernel": ["k_batched", "k_persistent"][dom],
-                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "kernel": "k_pool" + (" (shared-work pass)" if dom == 0 else " (exclusive pass)"),
+                "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)",
                 "kernel_ms": kms.tolist(), "kernel_alg_bytes": kbytes.tolist(),
-                "escalated_queries": st["escalated"]}
+                "escalated_queries": esc}
 
     # e2e: host arrays (pinned), copies inside the timed region
     hs = torch.from_numpy(s).pin_memory().numpy()
     ht = torch.from_numpy(t).pin_memory().numpy()
-    e2e_opt = fc.make_opts(sched=fc.SCHED_HEURISTIC, engine=fc.ENGINE_BATCHED)
-    fc.stcon_batch(G, hs, ht, opts=e2e_opt)
+    hg = torch.from_numpy(gi).pin_memory().numpy() if gi is not None else None
+    e2e_opt = fc.make_opts(sched=sched, engine=fc.ENGINE_BATCHED)
+    fc.stcon_batch(Gs, hs, ht, graph_idx=hg, opts=e2e_opt)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        conn, hops = fc.stcon_batch(G, hs, ht, opts=e2e_opt)
-    e2e_s = time.perf_counter() - t0
-    e2e_s = max_over_ranks(ws, e2e_s)
-    e2e = {"value": total_q / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * 4 * nq,
-           "d2h_bytes_per_step": 2 * 4 * nq}
-    exact = exact and bool((hops == hops_gpu).all())
+        conn, hops = fc.stcon_batch(Gs, hs, ht, graph_idx=hg, opts=e2e_opt)
+    e2e_s = reduce_over_ranks(ws, time.perf_counter() - t0, "max")
+    e2e = {"value": total_q / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (8 if gi is None else 12) * nq,
+           "d2h_bytes_per_step": 8 * nq}
+    exact = bool((hops == hops_gpu).all())
 
-    # plain level-synchronous form on a sample
+    # plain level-synchronous form and one-launch-per-query form, on samples
     plain_n = min(nq, 128 if cfg["kind"] != "grid" else 16)
+    samp = np.arange(plain_n) * max(1, nq // plain_n)
     popt = fc.make_opts(sched=fc.SCHED_PLAIN, engine=fc.ENGINE_HOSTLOOP)
     t0 = time.perf_counter()
-    pc, ph = fc.stcon_batch(G, s[:plain_n], t[:plain_n], opts=popt)
+    pc, ph = fc.stcon_batch(Gs, s[samp], t[samp], graph_idx=None if gi is None else gi[samp],
+                            opts=popt)
     plain_s = time.perf_counter() - t0
-    exact = exact and bool((ph == hops_gpu[:plain_n]).all())
+    exact = exact and bool((ph == hops_gpu[samp]).all())
     plain = {"value": plain_n / plain_s, "unit": UNIT, "sample": plain_n,
              "form": "host loop, one launch per level, alternating sides, top-down"}
+    sopt = fc.make_opts(sched=sched)
+    t0 = time.perf_counter()
+    for k in samp:
+        c1, h1 = Gs[0 if gi is None else gi[k]].stcon(int(s[k]), int(t[k]), sopt)
+        exact = exact and h1 == hops_gpu[k]
+    single_s = time.perf_counter() - t0
+    single = {"value": plain_n / single_s, "unit": UNIT, "sample": plain_n,
+              "form": "fc_stcon per query (one persistent launch each)"}
 
-    line = None
     if rank == 0:
         cpu = None
         if ws == 1:
-            rate, done, el = time_cpu_reference(rp, col, s, t, nthreads, min_seconds=10.0,
-                                                max_queries=4 * nthreads)
+            nthreads = os.cpu_count() or 1
+            # the oracle checks a sample of this very workload, then is timed
+            cs = np.arange(0, nq, max(1, nq // 16))
+            graphs_needed = None if gi is None else set(int(x) for x in np.unique(gi[cs]))
+            if gi is None:
+                csrs = [Gs[0].csr()]
+            else:
+                csrs = [Gs[k].csr() if k in graphs_needed else None for k in range(len(Gs))]
+            want = cpu_queries(csrs, gi, s, t, cs, nthreads)
+            exact = exact and bool((hops_gpu[cs] == want).all())
+            rate, done, el = cpu_rate(csrs, gi, s, t, nthreads, min_seconds=10.0,
+                                      max_queries=4 * nthreads, order=cs)
             cpu = {"value": rate, "unit": UNIT, "cores": nthreads, "kind": "port",
                    "sample": f"{done} queries of the workload ({el:.1f} s), one full BFS from s "
                              "per query (Graph::bfs restated in oracle/fc_oracle.c)"}
@@ -392,14 +451,14 @@ def run_fastcon(args, cfg):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": dict(config_desc(args.config, cfg), engine="batched",
-                           sched="heuristic", parallelism=f"replicas{ws}"),
+            "config": dict(config_desc(args.config, cfg, nq), engine="batched",
+                           sched=args.sched, parallelism=f"replicas{ws}"),
             "exact": exact,
             "gteps_inspected": ins / args.steps / (ms / args.steps / 1000.0) / 1e9,
             "edges_inspected_per_step": ins / args.steps,
-            "plain": plain,
+            "plain": plain, "one_launch_per_query": single,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": launches * args.steps,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -414,11 +473,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fastcon", choices=["fastcon", "reference"])
     ap.add_argument("--config", default="rmat24", choices=sorted(CONFIGS))
+    ap.add_argument("--sched", default="heuristic", choices=["heuristic", "plain", "learned"])
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
+    import oracle
+    oracle.build()
     if args.impl == "reference":
-        import oracle
-        oracle.build()
         run_reference(args, cfg)
     else:
         import importlib.util
@@ -427,8 +487,6 @@ def main():
         mod = importlib.util.module_from_spec(spec)
         spec.loader.exec_module(mod)
         mod.build()
-        import oracle
-        oracle.build()
         run_fastcon(args, cfg)
 
 

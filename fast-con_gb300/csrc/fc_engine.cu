@@ -627,12 +627,14 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
     FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 8 * sizeof(int), stream));
     if (engine == FC_ENGINE_BATCHED) {
         if ((rc = ensure_pool(c))) return rc;
-        int grid = pool_grid(c->sm_count, o.ctas_per_sm);
+        // two owner CTAs per SM: with tile sharing more owners do not help and
+        // each one costs a status array of the largest graph
+        int grid = pool_grid(c->sm_count, o.ctas_per_sm > 0 ? o.ctas_per_sm : 2);
         if (grid > c->p_grid) grid = c->p_grid;
         if (o.max_slots > 0 && o.max_slots < grid) grid = o.max_slots;
         // a slot's visit log bounds the queries it can finish itself; bigger
         // ones move to the exclusive pass below
-        int log_cap = (int)std::min<size_t>(maxnv, (size_t)1 << 22);
+        int log_cap = (int)std::min<size_t>(maxnv, (size_t)1 << 20);
         rc = ensure_batch_arena(c, (size_t)grid, maxnv, log_cap);
         if (rc) return rc;
         PoolArgs a;

@@ -223,6 +223,17 @@ def grid_pairs(w: int, h: int, count: int, seed: int, min_manhattan: int):
     return np.concatenate(out_s).astype(np.int32), np.concatenate(out_t).astype(np.int32)
 
 
+def batched_scales(count: int = 512, first_seed: int = 100, lo: int = 12, hi: int = 20):
+    """Scales of the many-graph workload: graph i (seed first_seed + i) has
+    scale lo + (hash(seed, 0x5CA1E, 0) mod (hi - lo + 1)), i.e. uniform in
+    [lo, hi]."""
+    out = []
+    for i in range(count):
+        h = int(hash64(first_seed + i, 0x5CA1E, np.array([0], dtype=np.uint64))[0])
+        out.append(lo + h % (hi - lo + 1))
+    return out
+
+
 def csr_from_edges(nv: int, u: np.ndarray, v: np.ndarray):
     """Canonical CSR in numpy (symmetrised, loops dropped, deduped, rows
     sorted) for small graphs in tests."""
