@@ -387,8 +387,17 @@ def run_fastcon(args, cfg):
     dom = int(np.argmax(kms))
     peak, peak_src = peaks()
     achieved = (kbytes[dom] / 1e9) / (kms[dom] / 1e3) if kms[dom] > 0 else 0.0
+    # DRAM traffic per launch: an ncu capture of a smaller case of the same
+    # kernel, scaled by the algorithmic bytes this launch processes
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic_per_unit.json")
+    if os.path.exists(tp):
+        ratio = json.load(open(tp)).get("k_pool", {}).get("dram_bytes_per_alg_byte")
+        if ratio:
+            traffic = float(ratio) * float(kbytes[dom])
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None,
+                "frac": achieved / peak, "traffic": traffic,
+                "traffic_source": "profiles/traffic_per_unit.json (scaled small-case capture)",
                 "kernel": "k_pool" + (" (shared-work pass)" if dom == 0 else " (exclusive pass)"),
                 "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)",
                 "kernel_ms": kms.tolist(), "kernel_alg_bytes": kbytes.tolist(),

@@ -633,8 +633,21 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         if (grid > c->p_grid) grid = c->p_grid;
         if (o.max_slots > 0 && o.max_slots < grid) grid = o.max_slots;
         // a slot's visit log bounds the queries it can finish itself; bigger
-        // ones move to the exclusive pass below
-        int log_cap = (int)std::min<size_t>(maxnv, (size_t)1 << 20);
+        // ones move to the exclusive pass below.  Full-size logs when the arena
+        // fits in 40% of the free device memory (deep graphs such as grids
+        // visit millions of vertices per query), otherwise as large as fits.
+        size_t sstride = (maxnv + 255) / 256 * 256;
+        size_t log_cap_sz = maxnv;
+        if (!(c->b_status && c->b_slots >= (size_t)grid && c->b_status_stride >= sstride &&
+              c->b_log_cap >= (int)maxnv)) {
+            size_t free_b = 0, total_b = 0;
+            cudaMemGetInfo(&free_b, &total_b);
+            size_t held = c->b_slots * (c->b_status_stride + 4 * (size_t)c->b_log_cap);
+            size_t budget = (size_t)(0.4 * (double)(free_b + held)) / (size_t)grid;
+            size_t fit = budget > sstride ? (budget - sstride) / 4 : 0;
+            if (fit < log_cap_sz) log_cap_sz = std::max<size_t>(fit, std::min<size_t>(maxnv, 1 << 16));
+        }
+        int log_cap = (int)log_cap_sz;
         rc = ensure_batch_arena(c, (size_t)grid, maxnv, log_cap);
         if (rc) return rc;
         PoolArgs a;

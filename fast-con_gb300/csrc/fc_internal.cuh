@@ -5,7 +5,7 @@
 //   col      int32[ne]       neighbours, rows sorted ascending, deduplicated
 //
 // Traversal state of one query slot:
-//   status   uint8[nv, padded to 16]   0xFF = unvisited, else side<<7 | min(level,127)
+//   status   uint8[nv, padded to 16]   0xFF = unvisited, else side<<7 | min(level,126)
 //   log      int32[nv]                 every claimed vertex exactly once; side 0
 //                                      appends upward from log[0], side 1 downward
 //                                      from log[nv-1], so a side's frontier is always
@@ -26,11 +26,15 @@
 namespace fc {
 
 constexpr uint8_t ST_UNVISITED = 0xFF;
-constexpr int LEVEL7_MAX = 126;  // bottom-up needs exact frontier codes: level+1 <= 126
+// Levels are stored clamped to 126, so side 1's largest code is 0xFE and never
+// equals ST_UNVISITED.  Bottom-up compares exact frontier codes, so it is used
+// only while level + 1 <= 125 (below the clamp).
+constexpr int LEVEL_CLAMP = 126;
+constexpr int LEVEL7_MAX = 125;
 
 __host__ __device__ inline uint8_t st_code(int side, int level)
 {
-    return (uint8_t)((side << 7) | (level < 127 ? level : 127));
+    return (uint8_t)((side << 7) | (level < LEVEL_CLAMP ? level : LEVEL_CLAMP));
 }
 
 struct DGraph {

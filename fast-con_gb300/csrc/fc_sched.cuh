@@ -76,7 +76,7 @@ __host__ __device__ inline void ql_start(QLocal &q, int two, int nv, long long n
 // Choose the next step.  allow_bu = 0 in the batched engine (a bottom-up step
 // scans every vertex, which one CTA must not do).  bu_level_cap limits
 // bottom-up to levels whose status code is exact (s-t status bytes hold
-// min(level, 127)).
+// min(level, 126)).
 __host__ __device__ inline void ql_decide(QLocal &q, int sched, int allow_bu, int bu_level_cap)
 {
     int side;

@@ -301,6 +301,35 @@ def test_batched_many_queries_rmat(fastcon_lib, oracle_mod):
 
 
 # --------------------------------------------------------------------------
+# deep graphs: both sides grow past 127 levels (status bytes clamp the level)
+# --------------------------------------------------------------------------
+def test_deep_levels_path_and_grid(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    n = 700
+    P = fc.Graph.from_edges(np.arange(n - 1), np.arange(1, n), n)
+    for eng in ENGINES_SINGLE:
+        for sch in SCHEDS:
+            o = opts(fc, eng, sch)
+            assert P.stcon(0, n - 1, o) == (True, n - 1), (eng, sch)
+            assert P.stcon(350, 3, o) == (True, 347), (eng, sch)
+            assert P.bfs_levels(0, o).tolist() == list(range(n)), (eng, sch)
+    w = h = 220
+    u, v = graphs.grid_edges(w, h, 0.05, 5, 3, 6)
+    G = fc.Graph.from_edges(u, v, w * h)
+    rp, col = oracle_mod.build_csr(w * h, u, v)
+    s, t = graphs.grid_pairs(w, h, 60, 7, 200)
+    _, want, _ = oracle_mod.stcon_batch(rp, col, s, t, nthreads=4)
+    assert want.max() > 260
+    for eng in ENGINES_BATCH:
+        for sch in SCHEDS:
+            conn, hops = fc.stcon_batch(G, s, t, opts=opts(fc, eng, sch))
+            assert (hops == want).all(), (eng, sch)
+    for k in range(0, 60, 13):
+        for eng in ENGINES_SINGLE:
+            assert G.stcon(s[k], t[k], opts(fc, eng, "heuristic")) == (want[k] >= 0, want[k])
+
+
+# --------------------------------------------------------------------------
 # the work-sharing engine with every step shared: tiles, row jobs for hub
 # rows longer than 8,192 entries, shared status resets
 # --------------------------------------------------------------------------
