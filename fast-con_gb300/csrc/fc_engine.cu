@@ -11,13 +11,10 @@
 //               at a bounded software grid barrier after every step (reference
 //               shape: BFSDispath + GlobalSync, K/.../BFS_WE_KernelDispatch.cu:
 //               17-38, whose barrier spins without bound).
-//   batched     one launch for many queries; each CTA pulls queries from a
-//               global counter and runs them privately with __syncthreads
-//               between steps (reference shape: one CTA per source in
-//               BFS_4K_BLOCK, BFS_4K_BLOCK/.../BFS_WE_Block.cu:33-147).  A query
-//               whose next step would exceed the CTA's work limit or log space
-//               is handed to a spill list that the persistent engine finishes
-//               in the same stream.
+//   batched     the work-sharing engine of fc_pool.cu (the default for every
+//               call): each CTA owns queries, big steps are shared as tiles.
+//               A query whose visit log could outgrow its slot is finished by
+//               a second, exclusive launch of the same kernel in the stream.
 //
 // s-t connectivity grows a ball from s (side 0) and from t (side 1), one side
 // per step.  With both balls complete and disjoint, the first edge from the
@@ -55,7 +52,12 @@ struct StepArgs {
     int32_t *log;
     int cap;
     TeamCounters *tc;
+    int variant;
 };
+
+// Engines without row splitting walk every row inside one CTA, so a
+// warp-centric step would leave a hub row to a single warp: use the hybrid.
+__host__ __device__ inline int unsplit_variant(int v) { return v == VAR_WARP ? VAR_HYBRID : v; }
 
 template <int T>
 __global__ void __launch_bounds__(T) k_step(StepArgs a)
@@ -63,7 +65,7 @@ __global__ void __launch_bounds__(T) k_step(StepArgs a)
     __shared__ SmemTopDown<T> sm;
     run_step<T>(a.mode, a.gp, a.side, a.dir, a.level, a.other_radius, a.log + a.front_begin, a.F,
                 blockIdx.x, gridDim.x, a.status, a.levels, a.log, a.cap, &a.tc->tail[a.side],
-                &a.tc->deg[a.side], &a.tc->found, &a.tc->inspected, sm);
+                &a.tc->deg[a.side], &a.tc->found, &a.tc->inspected, sm, unsplit_variant(a.variant));
 }
 
 // ---------------------------------------------------------------------------
@@ -78,7 +80,7 @@ struct PersistArgs {
     const int32_t *list;
     const int *list_count;
     int nlist;
-    int mode, sched;
+    int mode, sched, force_variant;
     uint8_t *status;
     int32_t *levels;
     int32_t *log;
@@ -119,7 +121,8 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
         __syncthreads();
         while (true) {
             if (threadIdx.x == 0 && !ql.done)
-                ql_decide(ql, a.sched, 1, a.mode == MODE_BFS ? 0x7fffffff : LEVEL7_MAX);
+                ql_decide(ql, a.sched, 1, a.mode == MODE_BFS ? 0x7fffffff : LEVEL7_MAX, 0,
+                          a.force_variant);
             __syncthreads();
             if (ql.done) break;
             int F;
@@ -127,7 +130,7 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
             const int32_t *front = ql_frontier(ql, a.log, nv, x, &F);
             run_step<T>(a.mode, gp, x, ql.dir, ql.radius[x], ql.radius[1 - x], front, F,
                         blockIdx.x, gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x],
-                        &tc->deg[x], &tc->found, &tc->inspected, sm);
+                        &tc->deg[x], &tc->found, &tc->inspected, sm, unsplit_variant(ql.variant));
             if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
             if (threadIdx.x == 0)
                 ql_update(ql, ld_cg(&tc->found), ld_cg(&tc->tail[x]), ld_cg_u64(&tc->deg[x]),
@@ -299,7 +302,7 @@ static int check_counters(DevCtx *c, cudaStream_t st)
 
 // Host-loop engine: one launch per step; returns the final QLocal.
 static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, int sched,
-                    QLocal *out, cudaStream_t st)
+                    QLocal *out, cudaStream_t st, int force_variant = -1)
 {
     constexpr int T = FC_BLOCK;
     const GraphPair gp = to_dev(gph);
@@ -315,7 +318,7 @@ static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, in
     if (per_sm < 1) per_sm = 1;
     const int full_grid = per_sm * c->sm_count;
     while (!q.done) {
-        ql_decide(q, sched, 1, mode == MODE_BFS ? 0x7fffffff : LEVEL7_MAX);
+        ql_decide(q, sched, 1, mode == MODE_BFS ? 0x7fffffff : LEVEL7_MAX, 0, force_variant);
         const int x = q.side;
         StepArgs a;
         a.gp = gp;
@@ -324,6 +327,7 @@ static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, in
         a.dir = q.dir;
         a.level = q.radius[x];
         a.other_radius = q.radius[1 - x];
+        a.variant = q.variant;
         a.F = q.tail[x] - q.head[x];
         a.front_begin = x == 0 ? q.head[0] : nv - q.tail[1];
         a.status = c->status;
@@ -343,6 +347,8 @@ static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, in
     *out = q;
     return FC_OK;
 }
+
+static int forced_variant(const fc_opts &o) { return o.variant > 0 ? o.variant - 1 : -1; }
 
 static void fill_stats(fc_stats *st, const QLocal &q, int launches)
 {
@@ -436,6 +442,7 @@ static PoolArgs pool_args_exclusive(DevCtx *c, int mode, const fc_opts &o)
     a.graphs = (const GraphPair *)c->d_graphs;
     a.mode = mode;
     a.sched = o.sched;
+    a.force_variant = forced_variant(o);
     a.exclusive = 1;
     a.slots = (PoolSlot *)c->p_slots;
     a.jobs = (RowJob *)c->p_jobs;
@@ -474,6 +481,7 @@ static int run_single(DevCtx *c, int mode, int engine, const GraphPairH &gp, int
         a.nlist = 1;
         a.mode = mode;
         a.sched = o.sched;
+        a.force_variant = forced_variant(o);
         a.status = c->status;
         a.levels = c->levels;
         a.log = c->log;
@@ -518,7 +526,7 @@ int engine_bfs(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_levels, co
     QLocal q;
     std::memset(&q, 0, sizeof(q));
     if (engine == FC_ENGINE_HOSTLOOP) {
-        rc = hostloop(c, MODE_BFS, gp, s, s, o.sched, &q, stream);
+        rc = hostloop(c, MODE_BFS, gp, s, s, o.sched, &q, stream, forced_variant(o));
     } else {
         rc = run_single(c, MODE_BFS, engine, gp, s, s, o, q, stream);
     }
@@ -548,7 +556,7 @@ int engine_stcon(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int32_t 
     QLocal q;
     std::memset(&q, 0, sizeof(q));
     if (engine == FC_ENGINE_HOSTLOOP) {
-        rc = hostloop(c, MODE_STCON, gp, s, t, o.sched, &q, stream);
+        rc = hostloop(c, MODE_STCON, gp, s, t, o.sched, &q, stream, forced_variant(o));
         if (rc) return rc;
         // clear the claimed status bytes (whole array: one memset)
         FC_CUDA_TRY(cudaMemsetAsync(c->status, 0xFF, (size_t)(nv + 15) / 16 * 16, stream));
@@ -659,6 +667,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.nlist = nq;
         a.mode = MODE_STCON;
         a.sched = o.sched;
+        a.force_variant = forced_variant(o);
         a.exclusive = 0;
         a.slots = (PoolSlot *)c->p_slots;
         a.jobs = (RowJob *)c->p_jobs;
@@ -701,6 +710,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.nlist = nq;
         a.mode = MODE_STCON;
         a.sched = o.sched;
+        a.force_variant = forced_variant(o);
         a.status = c->status;
         a.levels = c->levels;
         a.log = c->log;
@@ -730,7 +740,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
                 continue;
             }
             QLocal q;
-            rc = hostloop(c, MODE_STCON, g, hs[i], ht[i], o.sched, &q, stream);
+            rc = hostloop(c, MODE_STCON, g, hs[i], ht[i], o.sched, &q, stream, forced_variant(o));
             if (rc) return rc;
             FC_CUDA_TRY(cudaMemsetAsync(c->status, 0xFF, (size_t)(g.fwd.nv + 15) / 16 * 16, stream));
             hc[i] = q.connected;

@@ -16,9 +16,10 @@
 //
 // Claiming: slot.next packs {seq:20, ntiles:22, next tile:22} in one 64-bit
 // word.  The owner publishes a step by writing its description and then
-// storing a new seq (release).  A helper claims tile i of step seq with a CAS
-// on the whole word, so a claim can never land on a newer step; the owner
-// itself claims with atomicAdd.  A row job adds one to ntiles with an atomic
+// storing a new seq (release).  Every CTA, the owner included, claims tile i
+// of step seq with a CAS on the whole word, so a claim can never land on a
+// newer step and the tile counter never passes ntiles.  A row job adds one to
+// ntiles with an atomic
 // add on the same word after writing its descriptor; a helper that claims a
 // job waits (bounded) for the descriptor's seq stamp.  The step is complete
 // when `done` (read first) equals ntiles (read second).
@@ -61,7 +62,7 @@ struct RowJob {
 
 // Step description: written by the owner before it publishes the step.
 struct PoolDesc {
-    int q, gidx, mode, side, dir, level, other_radius, F, front_off, nvt, cap, nreset;
+    int q, gidx, mode, side, dir, level, other_radius, F, front_off, nvt, cap, nreset, variant;
     uint8_t *status;
     int32_t *levels;
     int32_t *log;
@@ -116,6 +117,21 @@ struct SmemPool {
     int err;
     unsigned long long t_idle;
 };
+
+// Expand the tile's rows (one per thread) with the step's variant; rows longer
+// than a row job go to the sink in every variant.
+template <int T, class Vis>
+__device__ __forceinline__ void pool_expand(int variant, const int32_t *__restrict__ col, int rb,
+                                            int re, const Vis &vis, const AppendTarget &app,
+                                            SmemTopDown<T> &td, const SlotSink &sink)
+{
+    if (variant == VAR_WARP)
+        expand_warp(col, rb, re, vis, app, sink, POOL_SPLIT_E);
+    else if (variant == VAR_THREAD)
+        expand_thread(col, rb, re, vis, app, sink, POOL_SPLIT_E);
+    else
+        expand_rows<T>(col, rb, re, vis, app, td, sink);
+}
 
 // ---------------------------------------------------------------------------
 // One tile of a published step (any CTA).  sm.d holds the step description.
@@ -187,10 +203,10 @@ __device__ void pool_tile(const PoolArgs &a, PoolSlot *slot, int tile, unsigned 
         SlotSink sink{slot, a.jobs + (size_t)(slot - a.slots) * POOL_JOBS, seq};
         if (d.mode == MODE_BFS) {
             VisitBFS vis{d.levels, d.level + 1};
-            expand_rows<T>(gx.col, rb, re, vis, app, sm.td, sink);
+            pool_expand<T>(d.variant, gx.col, rb, re, vis, app, sm.td, sink);
         } else {
             VisitSTCON vis{d.status, st_code(d.side, d.level + 1), d.side, &slot->tc.found};
-            expand_rows<T>(gx.col, rb, re, vis, app, sm.td, sink);
+            pool_expand<T>(d.variant, gx.col, rb, re, vis, app, sm.td, sink);
         }
         return;
     }
@@ -385,7 +401,8 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
     desc.nreset = 0;
     while (true) {
         if (tid == 0 && !sm.ql.done) {
-            ql_decide(sm.ql, a.sched, 1, a.mode == MODE_BFS ? INT_MAX : LEVEL7_MAX);
+            ql_decide(sm.ql, a.sched, 1, a.mode == MODE_BFS ? INT_MAX : LEVEL7_MAX, 1,
+                      a.force_variant);
             const int x = sm.ql.side;
             const long long m = (long long)(sm.ql.dt[x] - sm.ql.dh[x]);
             if (!a.exclusive && (long long)sm.ql.tail[0] + sm.ql.tail[1] + m > cap) {
@@ -402,11 +419,12 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
         if (!sm.publish) {
             run_step<T>(a.mode, gp, x, DIR_TD, sm.ql.radius[x], sm.ql.radius[1 - x], front, F, 0, 1,
                         status, levels, log, cap, &my->tc.tail[x], &my->tc.deg[x], &my->tc.found,
-                        &my->tc.inspected, sm.td);
+                        &my->tc.inspected, sm.td, sm.ql.variant);
             __syncthreads();
         } else {
             desc.side = x;
             desc.dir = sm.ql.dir;
+            desc.variant = sm.ql.variant;
             desc.level = sm.ql.radius[x];
             desc.other_radius = sm.ql.radius[1 - x];
             desc.F = F;

@@ -20,7 +20,7 @@ struct PoolArgs {
     const int32_t *list;      // optional subset of query indices
     const int *list_count;    // device count of list entries (nullable)
     int nlist;                // count when list_count is NULL
-    int mode, sched;
+    int mode, sched, force_variant;
     int exclusive;            // 1: CTA 0 owns every query in turn, arrays span the graph
     PoolSlot *slots;          // one per CTA
     RowJob *jobs;             // POOL_JOBS per CTA

@@ -73,11 +73,20 @@ __host__ __device__ inline void ql_start(QLocal &q, int two, int nv, long long n
     }
 }
 
-// Choose the next step.  allow_bu = 0 in the batched engine (a bottom-up step
-// scans every vertex, which one CTA must not do).  bu_level_cap limits
-// bottom-up to levels whose status code is exact (s-t status bytes hold
-// min(level, 126)).
-__host__ __device__ inline void ql_decide(QLocal &q, int sched, int allow_bu, int bu_level_cap)
+// Expansion variants of a top-down step (answers never depend on them):
+enum {
+    VAR_HYBRID = 0,  // CTA / warp / scan classes per row length (CTA barriers)
+    VAR_WARP = 1,    // warp-centric, no CTA barriers
+    VAR_THREAD = 2,  // one lane per row
+};
+
+// Choose the next step.  allow_bu = 0 where a bottom-up step would be run by
+// one CTA (it scans every vertex).  bu_level_cap limits bottom-up to levels
+// whose status code is exact (s-t status bytes hold min(level, 126)).
+// long_rows_split: the engine hands very long rows to many CTAs, so the
+// warp-centric variant is safe for frontiers with hubs.
+__host__ __device__ inline void ql_decide(QLocal &q, int sched, int allow_bu, int bu_level_cap,
+                                          int long_rows_split = 0, int force_variant = -1)
 {
     int side;
     if (!q.two)
@@ -90,7 +99,15 @@ __host__ __device__ inline void ql_decide(QLocal &q, int sched, int allow_bu, in
     }
     q.side = side;
     q.dir = DIR_TD;
-    q.variant = 0;
+    q.variant = VAR_HYBRID;
+    if (sched != FC_SCHED_PLAIN) {
+        const long long nf = q.tail[side] - q.head[side];
+        const long long mf = (long long)(q.dt[side] - q.dh[side]);
+        if (mf < 8 * nf)
+            q.variant = VAR_THREAD;  // low, even degrees: one lane per row
+        else if (long_rows_split)
+            q.variant = VAR_WARP;
+    }
     if (sched != FC_SCHED_PLAIN && allow_bu && q.radius[side] + 1 <= bu_level_cap) {
         long long mf = (long long)(q.dt[side] - q.dh[side]);
         long long unexplored = q.ne - (long long)(q.dt[0] + q.dt[1]);
@@ -98,6 +115,7 @@ __host__ __device__ inline void ql_decide(QLocal &q, int sched, int allow_bu, in
         // Beamer, Asanovic & Patterson (SC'12) thresholds: alpha = 14, beta = 24
         if (mf * 14 > unexplored && nf * 24 > q.nv) q.dir = DIR_BU;
     }
+    if (force_variant >= 0) q.variant = force_variant;
 }
 
 // Advance after the step on q.side finished (counters final).
@@ -150,24 +168,40 @@ __device__ __forceinline__ const int32_t *ql_frontier(const QLocal &q, const int
 // ---------------------------------------------------------------------------
 // One step for a team of CTAs.
 // ---------------------------------------------------------------------------
+template <int T, class Vis>
+__device__ __forceinline__ void topdown_variant(int variant, const DGraph &gx,
+                                                const int32_t *frontier, int F, int team_rank,
+                                                int team_size, const Vis &vis,
+                                                const AppendTarget &app, SmemTopDown<T> &sm,
+                                                const int *stop)
+{
+    if (variant == VAR_WARP)
+        topdown_warps<T, VAR_WARP>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis,
+                                   app, stop);
+    else if (variant == VAR_THREAD)
+        topdown_warps<T, VAR_THREAD>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis,
+                                     app, stop);
+    else
+        topdown_step<T>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis, app, sm, stop);
+}
+
 template <int T>
 __device__ void run_step(int mode, const GraphPair &gp, int side, int dir, int level,
                          int other_radius, const int32_t *frontier, int F, int team_rank,
                          int team_size, uint8_t *status, int32_t *levels, int32_t *log, int cap,
                          int *tail_ctr, unsigned long long *deg_ctr, int *found,
-                         unsigned long long *bu_ins, SmemTopDown<T> &sm)
+                         unsigned long long *bu_ins, SmemTopDown<T> &sm, int variant = VAR_HYBRID)
 {
     const DGraph &gx = side ? gp.rev : gp.fwd;
     AppendTarget app{log, cap, side, tail_ctr, deg_ctr, gx.row_ptr};
     if (dir == DIR_TD) {
         if (mode == MODE_BFS) {
             VisitBFS vis{levels, level + 1};
-            topdown_step<T>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis, app, sm,
-                            nullptr);
+            topdown_variant<T>(variant, gx, frontier, F, team_rank, team_size, vis, app, sm,
+                               nullptr);
         } else {
             VisitSTCON vis{status, st_code(side, level + 1), side, found};
-            topdown_step<T>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis, app, sm,
-                            found);
+            topdown_variant<T>(variant, gx, frontier, F, team_rank, team_size, vis, app, sm, found);
         }
     } else {
         const DGraph &gr = side ? gp.fwd : gp.rev;

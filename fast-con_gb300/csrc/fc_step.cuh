@@ -17,6 +17,8 @@
 // log with a warp ballot/shuffle scan and one atomicAdd per warp.
 #pragma once
 
+#include <climits>
+
 #include "fc_internal.cuh"
 
 namespace fc {
@@ -229,6 +231,110 @@ __device__ __forceinline__ void expand_rows(const int32_t *__restrict__ col, int
             warp_append<1>(c, app);
         }
         __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Variant 1, warp-centric: the warp expands the rows of its 32 lanes without
+// any CTA barrier.  Rows longer than `big` go to the sink (row jobs) when it
+// takes them; rows of >= 32 entries are walked by the whole warp; shorter
+// rows are flattened by a warp prefix scan, and each lane finds the row of
+// its edge by a 5-step shuffle search over the scan.
+// ---------------------------------------------------------------------------
+template <class Vis, class Sink>
+__device__ __forceinline__ void expand_warp(const int32_t *__restrict__ col, int rb, int re,
+                                            const Vis &vis, const AppendTarget &app,
+                                            const Sink &sink, int big)
+{
+    const int lane = (int)lane_id();
+    if (re - rb > big && sink.push_row(rb, re)) rb = re;
+    while (true) {
+        unsigned m = __ballot_sync(0xffffffffu, re - rb >= 32);
+        if (!m) break;
+        int leader = __ffs(m) - 1;
+        int b = __shfl_sync(0xffffffffu, rb, leader);
+        int e = __shfl_sync(0xffffffffu, re, leader);
+        if (lane == leader) rb = re;
+        walk_range(col, b, e, lane, 32, vis, app);
+    }
+    const int d = re - rb;
+    const int incl = warp_inclusive_scan(d);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl = incl - d;
+    for (int base = 0; base < total; base += 32) {
+        const int e = base + lane;
+        int pos = 0;  // number of lanes whose rows end at or before edge e
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) {
+            int v = __shfl_sync(0xffffffffu, incl, pos + s - 1);
+            if (v <= e) pos += s;
+        }
+        const int owner = pos < 32 ? pos : 31;
+        const int ob = __shfl_sync(0xffffffffu, rb, owner);
+        const int oe = __shfl_sync(0xffffffffu, excl, owner);
+        int c[1] = {-1};
+        if (e < total) c[0] = vis.visit(__ldg(col + ob + (e - oe)));
+        warp_append<1>(c, app);
+    }
+}
+
+// Variant 2, thread per vertex: every lane walks its own row; the warp loop
+// runs to the longest row of the 32 (best for uniform low degrees).  Rows of
+// 64 or more entries are walked by the whole warp first, so no lane walks a
+// long row alone.
+template <class Vis, class Sink>
+__device__ __forceinline__ void expand_thread(const int32_t *__restrict__ col, int rb, int re,
+                                              const Vis &vis, const AppendTarget &app,
+                                              const Sink &sink, int big)
+{
+    const int lane = (int)lane_id();
+    if (re - rb > big && sink.push_row(rb, re)) rb = re;
+    while (true) {
+        unsigned m = __ballot_sync(0xffffffffu, re - rb >= 64);
+        if (!m) break;
+        int leader = __ffs(m) - 1;
+        int b = __shfl_sync(0xffffffffu, rb, leader);
+        int e = __shfl_sync(0xffffffffu, re, leader);
+        if (lane == leader) rb = re;
+        walk_range(col, b, e, lane, 32, vis, app);
+    }
+    const int len = re - rb;
+    int mx = len;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    for (int k = 0; k < mx; ++k) {
+        int c[1] = {-1};
+        if (k < len) c[0] = vis.visit(__ldg(col + rb + k));
+        warp_append<1>(c, app);
+    }
+}
+
+// Top-down step for variants 1 and 2: 32-vertex chunks dealt to the team's
+// warps; `stop_flag` is polled by each warp once per chunk.
+template <int T, int VARIANT, class Vis>
+__device__ void topdown_warps(const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
+                              const int32_t *frontier, int F, int team_rank, int team_size,
+                              const Vis &vis, const AppendTarget &app, const int *stop_flag)
+{
+    const int lane = (int)lane_id(), wid = threadIdx.x >> 5;
+    constexpr int W = T / 32;
+    const long long step = (long long)team_size * W;
+    for (long long chunk = (long long)team_rank * W + wid; chunk * 32 < F; chunk += step) {
+        if (stop_flag) {
+            int st = lane == 0 ? *(volatile const int *)stop_flag : 0;
+            if (__shfl_sync(0xffffffffu, st, 0)) break;
+        }
+        const long long i = chunk * 32 + lane;
+        int rb = 0, re = 0;
+        if (i < F) {
+            int u = ld_cg(frontier + i);
+            rb = __ldg(row_ptr + u);
+            re = __ldg(row_ptr + u + 1);
+        }
+        if (VARIANT == 1)
+            expand_warp(col, rb, re, vis, app, NoSink{}, INT_MAX);
+        else
+            expand_thread(col, rb, re, vis, app, NoSink{}, INT_MAX);
     }
 }
 

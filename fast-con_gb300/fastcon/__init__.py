@@ -52,7 +52,8 @@ class Opts(ctypes.Structure):
     _fields_ = [("sched", ctypes.c_int32), ("engine", ctypes.c_int32), ("block", ctypes.c_int32),
                 ("ctas_per_sm", ctypes.c_int32), ("use_graph", ctypes.c_int32),
                 ("max_slots", ctypes.c_int32), ("stream", ctypes.c_void_p),
-                ("cta_work_k", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+                ("cta_work_k", ctypes.c_int32), ("variant", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
 
 
 class Stats(ctypes.Structure):
@@ -134,13 +135,15 @@ def _i32(a):
 
 
 def make_opts(sched=SCHED_HEURISTIC, engine=ENGINE_AUTO, block=0, ctas_per_sm=0, use_graph=0,
-              max_slots=0, stream=None, cta_work_k=0) -> Opts:
+              max_slots=0, stream=None, cta_work_k=0, variant=0) -> Opts:
+    """variant: 0 = chosen by the schedule, 1 hybrid, 2 warp-centric, 3 lane per row."""
     o = Opts()
     lib().fc_opts_init(ctypes.byref(o))
     o.sched, o.engine, o.block, o.ctas_per_sm = sched, engine, block, ctas_per_sm
     o.use_graph, o.max_slots = use_graph, max_slots
     o.stream = stream
     o.cta_work_k = cta_work_k
+    o.variant = variant
     return o
 
 

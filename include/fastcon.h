@@ -70,7 +70,10 @@ typedef struct fc_opts {
                              tiles that every CTA may take (0 = 16 for
                              batches, 4 for single queries; < 0 = share
                              every step)                                    */
-    int32_t reserved[7];
+    int32_t variant;      /* top-down expansion variant: 0 = chosen by the
+                             schedule, 1 = CTA/warp/scan hybrid, 2 = warp-
+                             centric, 3 = one lane per row                  */
+    int32_t reserved[6];
 } fc_opts;
 
 typedef struct fc_stats {

@@ -301,6 +301,41 @@ def test_batched_many_queries_rmat(fastcon_lib, oracle_mod):
 
 
 # --------------------------------------------------------------------------
+# every expansion variant, forced, on every engine (answers never change)
+# --------------------------------------------------------------------------
+@pytest.mark.parametrize("variant", [1, 2, 3])
+def test_forced_variants(fastcon_lib, oracle_mod, variant):
+    fc = fastcon_lib
+    cases = []
+    u, v = graphs.rmat_edges(14, 8 << 14, seed=51, perm_seed=52)
+    cases.append((1 << 14, u, v))
+    u, v = graphs.grid_edges(90, 70, 0.05, 5, 4, 6)
+    cases.append((90 * 70, u, v))
+    nv = 40000  # a 20,000-leaf hub next to random edges
+    rng = np.random.default_rng(4)
+    u = np.concatenate([np.zeros(20000), rng.integers(0, nv, 30000)]).astype(np.int32)
+    v = np.concatenate([np.arange(1, 20001), rng.integers(0, nv, 30000)]).astype(np.int32)
+    cases.append((nv, u, v))
+    for nv, u, v in cases:
+        G = fc.Graph.from_edges(u, v, nv)
+        rp, col = oracle_mod.build_csr(nv, u, v)
+        s, t = graphs.uniform_pairs(nv, 150, seed=53)
+        _, want, _ = oracle_mod.stcon_batch(rp, col, s, t, nthreads=4)
+        for eng in ENGINES_BATCH:
+            for work_k in (0, -1):
+                o = fc.make_opts(sched=fc.SCHED_HEURISTIC, engine=opts(fc, eng).engine,
+                                 cta_work_k=work_k, variant=variant)
+                conn, hops = fc.stcon_batch(G, s, t, opts=o)
+                assert (hops == want).all(), (nv, eng, work_k)
+        for eng in ENGINES_SINGLE:
+            o = fc.make_opts(sched=fc.SCHED_HEURISTIC, engine=opts(fc, eng).engine, variant=variant)
+            for k in range(0, 150, 29):
+                assert G.stcon(s[k], t[k], o) == (want[k] >= 0, want[k]), (nv, eng)
+            lev, _ = oracle_mod.bfs_levels(rp, col, s[0])
+            assert (G.bfs_levels(s[0], o) == lev).all(), (nv, eng)
+
+
+# --------------------------------------------------------------------------
 # deep graphs: both sides grow past 127 levels (status bytes clamp the level)
 # --------------------------------------------------------------------------
 def test_deep_levels_path_and_grid(fastcon_lib, oracle_mod):
