@@ -667,6 +667,41 @@ int fc_stcon_batch_device(fc_graph *const *gs, int32_t ngraphs, const int32_t *d
                                   d_hops, o, stats, pick_stream(opts, L.c), stats != nullptr);
 }
 
+int fc_stcon_batch_scripted(fc_graph *g, const int32_t *d_s, const int32_t *d_t, int32_t nq,
+                            const uint8_t *d_script, int32_t script_len, const fc_opts *opts,
+                            int32_t *d_hops, int64_t *d_inspected, int32_t *d_trace,
+                            int32_t trace_cap, int32_t *d_trace_count)
+{
+    if (validate_ptr(g, "g") || validate_ptr(d_s, "s") || validate_ptr(d_t, "t") ||
+        validate_ptr(d_hops, "hops"))
+        return FC_ERR_INVALID;
+    if (nq < 0 || script_len < 0 || (d_script && script_len == 0) || (d_trace && !d_trace_count) ||
+        trace_cap < 0)
+        return FC_ERR_INVALID;
+    if (nq == 0) return FC_OK;
+    fc_opts o = opts ? *opts : default_opts();
+    o.engine = FC_ENGINE_BATCHED;
+    CtxLock L;
+    if (!L.c) return L.rc;
+    cudaStream_t st = pick_stream(opts, L.c);
+    int32_t *dc = nullptr;
+    FC_CUDA_TRY(cudaMallocAsync(&dc, sizeof(int32_t) * (size_t)nq, st));
+    if (d_trace_count) FC_CUDA_TRY(cudaMemsetAsync(d_trace_count, 0, sizeof(int32_t), st));
+    fc::BatchExtras ex;
+    ex.script = d_script;
+    ex.script_len = d_script ? script_len : 0;
+    ex.trace = d_trace;
+    ex.trace_cap = trace_cap;
+    ex.trace_count = d_trace_count;
+    ex.inspected = reinterpret_cast<long long *>(d_inspected);
+    fc::GraphPairH p = pair_of(g);
+    int rc = fc::engine_stcon_batch(L.c, &p, 1, nullptr, d_s, d_t, nq, dc, d_hops, o, nullptr, st,
+                                    true, &ex);
+    cudaFreeAsync(dc, st);
+    cudaStreamSynchronize(st);
+    return rc;
+}
+
 int fc_stcon_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *graph_idx, const int32_t *s,
                    const int32_t *t, int32_t nq, int32_t *connected, int32_t *hops,
                    const fc_opts *opts, fc_stats *stats)

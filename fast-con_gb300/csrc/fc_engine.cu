@@ -53,6 +53,7 @@ struct StepArgs {
     int cap;
     TeamCounters *tc;
     int variant;
+    unsigned long long *hist;  // degree-bin counters of the side (learned schedule)
 };
 
 // Engines without row splitting walk every row inside one CTA, so a
@@ -65,7 +66,8 @@ __global__ void __launch_bounds__(T) k_step(StepArgs a)
     __shared__ SmemTopDown<T> sm;
     run_step<T>(a.mode, a.gp, a.side, a.dir, a.level, a.other_radius, a.log + a.front_begin, a.F,
                 blockIdx.x, gridDim.x, a.status, a.levels, a.log, a.cap, &a.tc->tail[a.side],
-                &a.tc->deg[a.side], &a.tc->found, &a.tc->inspected, sm, unsplit_variant(a.variant));
+                &a.tc->deg[a.side], &a.tc->found, &a.tc->inspected, sm, unsplit_variant(a.variant),
+                a.hist);
 }
 
 // ---------------------------------------------------------------------------
@@ -88,6 +90,7 @@ struct PersistArgs {
     int32_t *out_conn;
     int32_t *out_hops;
     QueryStat *qstat;
+    const float *mlp;  // learned schedule weights (nullable)
 };
 
 template <int T>
@@ -119,10 +122,18 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
             ql_start(ql, a.mode == MODE_STCON, nv, gp.fwd.ne, s, t, ld_cg_u64(&tc->deg[0]),
                      ld_cg_u64(&tc->deg[1]));
         __syncthreads();
+        const int bu_cap = a.mode == MODE_BFS ? 0x7fffffff : LEVEL7_MAX;
         while (true) {
-            if (threadIdx.x == 0 && !ql.done)
-                ql_decide(ql, a.sched, 1, a.mode == MODE_BFS ? 0x7fffffff : LEVEL7_MAX, 0,
-                          a.force_variant);
+            if (threadIdx.x == 0 && !ql.done) {
+                ql_decide(ql, a.sched, 1, bu_cap, 0, a.force_variant);
+                if (a.mlp) {  // every CTA computes the same decision
+                    float f[MLP_IN], o[MLP_OUT];
+                    ql_features(ql, f);
+                    mlp_forward_scalar(a.mlp, f, o);
+                    ql_apply_logits(ql, o, 1, bu_cap);
+                    if (a.force_variant >= 0) ql.variant = a.force_variant;
+                }
+            }
             __syncthreads();
             if (ql.done) break;
             int F;
@@ -130,11 +141,18 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
             const int32_t *front = ql_frontier(ql, a.log, nv, x, &F);
             run_step<T>(a.mode, gp, x, ql.dir, ql.radius[x], ql.radius[1 - x], front, F,
                         blockIdx.x, gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x],
-                        &tc->deg[x], &tc->found, &tc->inspected, sm, unsplit_variant(ql.variant));
+                        &tc->deg[x], &tc->found, &tc->inspected, sm, unsplit_variant(ql.variant),
+                        a.mlp ? tc->hist[x] : nullptr);
             if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
-            if (threadIdx.x == 0)
+            if (threadIdx.x == 0) {
                 ql_update(ql, ld_cg(&tc->found), ld_cg(&tc->tail[x]), ld_cg_u64(&tc->deg[x]),
                           ld_cg_u64(&tc->inspected));
+                if (a.mlp) {
+                    unsigned long long h3[3];
+                    for (int b = 0; b < 3; ++b) h3[b] = ld_cg_u64(&tc->hist[x][b]);
+                    ql_update_hist(ql, x, h3);
+                }
+            }
             __syncthreads();
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) write_result(q, ql, a.out_conn, a.out_hops, a.qstat, 0);
@@ -317,8 +335,17 @@ static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, in
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step<T>, T, 0);
     if (per_sm < 1) per_sm = 1;
     const int full_grid = per_sm * c->sm_count;
+    const int bu_cap = mode == MODE_BFS ? 0x7fffffff : LEVEL7_MAX;
+    const bool learned = sched == FC_SCHED_LEARNED && c->mlp_ready;
     while (!q.done) {
-        ql_decide(q, sched, 1, mode == MODE_BFS ? 0x7fffffff : LEVEL7_MAX, 0, force_variant);
+        ql_decide(q, sched, 1, bu_cap, 0, force_variant);
+        if (learned) {
+            float f[MLP_IN], o[MLP_OUT];
+            ql_features(q, f);
+            mlp_forward_scalar(c->h_mlp, f, o);
+            ql_apply_logits(q, o, 1, bu_cap);
+            if (force_variant >= 0) q.variant = force_variant;
+        }
         const int x = q.side;
         StepArgs a;
         a.gp = gp;
@@ -335,6 +362,7 @@ static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, in
         a.log = c->log;
         a.cap = nv;
         a.tc = c->tc;
+        a.hist = learned ? c->tc->hist[x] : nullptr;
         int grid = q.dir == DIR_TD ? (a.F + T - 1) / T : full_grid;
         if (grid > full_grid) grid = full_grid;
         if (grid < 1) grid = 1;
@@ -343,6 +371,7 @@ static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, in
         FC_CUDA_TRY(cudaMemcpyAsync(c->h_tc, c->tc, sizeof(TeamCounters), cudaMemcpyDeviceToHost, st));
         FC_CUDA_TRY(cudaStreamSynchronize(st));
         ql_update(q, c->h_tc->found, c->h_tc->tail[x], c->h_tc->deg[x], c->h_tc->inspected);
+        if (learned) ql_update_hist(q, x, c->h_tc->hist[x]);
     }
     *out = q;
     return FC_OK;
@@ -432,7 +461,14 @@ static long long private_edges_default(const fc_opts &o, bool exclusive)
     // a negative setting shares every step
     if (o.cta_work_k < 0) return 0;
     if (o.cta_work_k > 0) return (long long)o.cta_work_k * 1024;
-    return exclusive ? 4096 : 16 * 1024;
+    return exclusive ? 4096 : 8 * 1024;
+}
+
+// Device weights when the learned schedule is asked for and weights are loaded;
+// without weights the learned schedule falls back to the heuristic.
+static const float *learned_weights(DevCtx *c, const fc_opts &o)
+{
+    return (o.sched == FC_SCHED_LEARNED && c->mlp_ready) ? c->d_mlp : nullptr;
 }
 
 static PoolArgs pool_args_exclusive(DevCtx *c, int mode, const fc_opts &o)
@@ -453,7 +489,19 @@ static PoolArgs pool_args_exclusive(DevCtx *c, int mode, const fc_opts &o)
     a.private_edges = private_edges_default(o, true);
     a.ctr = c->b_ctr;
     a.qstat = c->qstat;
+    a.mlp = learned_weights(c, o);
     return a;
+}
+
+static void apply_extras(PoolArgs &a, const BatchExtras *ex)
+{
+    if (!ex) return;
+    a.script = ex->script;
+    a.script_len = ex->script_len;
+    a.trace = ex->trace;
+    a.trace_cap = ex->trace_cap;
+    a.trace_count = ex->trace_count;
+    a.out_inspected = ex->inspected;
 }
 
 static int pick_engine(const fc_opts &o, int dflt)
@@ -489,6 +537,7 @@ static int run_single(DevCtx *c, int mode, int engine, const GraphPairH &gp, int
         a.out_conn = c->d_tmp_q + 2;
         a.out_hops = c->d_tmp_q + 3;
         a.qstat = c->qstat;
+        a.mlp = learned_weights(c, o);
         rc = launch_persistent<FC_BLOCK>(c, a, stream);
         if (rc) return rc;
         rc = check_counters(c, stream);
@@ -609,10 +658,14 @@ static int ensure_batch_arena(DevCtx *c, size_t slots, size_t maxnv, int log_cap
 int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int32_t *d_gi,
                        const int32_t *d_s, const int32_t *d_t, int32_t nq, int32_t *d_conn,
                        int32_t *d_hops, const fc_opts &o, fc_stats *st, cudaStream_t stream,
-                       bool sync)
+                       bool sync, const BatchExtras *ex)
 {
     constexpr int T = FC_BLOCK;
     if (nq <= 0) return FC_OK;
+    if (ex && pick_engine(o, FC_ENGINE_BATCHED) != FC_ENGINE_BATCHED) {
+        set_error("scripts and traces need the batched engine");
+        return FC_ERR_UNSUPPORTED;
+    }
     size_t maxnv = 1;
     for (int i = 0; i < ngraphs; ++i)
         if ((size_t)gps[i].fwd.nv > maxnv) maxnv = (size_t)gps[i].fwd.nv;
@@ -682,6 +735,8 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.out_conn = d_conn;
         a.out_hops = d_hops;
         a.qstat = c->qstat;
+        a.mlp = learned_weights(c, o);
+        apply_extras(a, ex);
         rc = pool_launch(a, grid, stream);
         if (rc) return rc;
         FC_CUDA_TRY(cudaEventRecord(c->evm, stream));
@@ -694,6 +749,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         x.list_count = c->b_ctr + 2;
         x.out_conn = d_conn;
         x.out_hops = d_hops;
+        apply_extras(x, ex);
         // same counter block: next and finished restart at 0, the spill count
         // ([2]) and the error / invalid flags carry over
         FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 2 * sizeof(int), stream));
@@ -718,6 +774,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.out_conn = d_conn;
         a.out_hops = d_hops;
         a.qstat = c->qstat;
+        a.mlp = learned_weights(c, o);
         rc = launch_persistent<T>(c, a, stream);
         if (rc) return rc;
         FC_CUDA_TRY(cudaEventRecord(c->evm, stream));

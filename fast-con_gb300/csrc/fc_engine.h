@@ -57,6 +57,10 @@ struct DevCtx {
     void *p_slots = nullptr;
     void *p_jobs = nullptr;
     int p_grid = 0;
+    // learned schedule weights (1,703 floats), device and host copies
+    float *d_mlp = nullptr;
+    float h_mlp[1703];
+    int mlp_ready = 0;
     int b_log_cap = 0;
     int *b_ctr = nullptr;            // [0] next query, [1] spill count, [2] error
     int32_t *b_spill = nullptr;
@@ -80,10 +84,20 @@ int engine_bfs(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_levels,
 int engine_stcon(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int32_t *conn,
                  int32_t *hops, const fc_opts &o, fc_stats *st, cudaStream_t stream);
 
+// Training-data hooks of the batched engine (all device pointers, nullable).
+struct BatchExtras {
+    const unsigned char *script = nullptr;  // nq * script_len action bytes
+    int script_len = 0;
+    int32_t *trace = nullptr;               // trace_cap records of 24 ints
+    int trace_cap = 0;
+    int32_t *trace_count = nullptr;
+    long long *inspected = nullptr;         // per query
+};
+
 int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int32_t *d_gi,
                        const int32_t *d_s, const int32_t *d_t, int32_t nq, int32_t *d_conn,
                        int32_t *d_hops, const fc_opts &o, fc_stats *st, cudaStream_t stream,
-                       bool sync);
+                       bool sync, const BatchExtras *ex = nullptr);
 
 void set_error(const char *fmt, ...);
 

@@ -63,6 +63,8 @@ struct RowJob {
 // Step description: written by the owner before it publishes the step.
 struct PoolDesc {
     int q, gidx, mode, side, dir, level, other_radius, F, front_off, nvt, cap, nreset, variant;
+    int tile_mult;  // top-down tiles hold tile_mult chunks of T frontier vertices
+    int track_hist; // count claimed vertices per degree bin (learned schedule)
     uint8_t *status;
     int32_t *levels;
     int32_t *log;
@@ -115,7 +117,7 @@ struct SmemPool {
     int q, li, publish, flag, cand, claimed, cursor;
     unsigned seq, my_seq;
     int err;
-    unsigned long long t_idle;
+    unsigned long long t_idle, t_step;
 };
 
 // Expand the tile's rows (one per thread) with the step's variant; rows longer
@@ -159,7 +161,7 @@ __device__ void pool_tile(const PoolArgs &a, PoolSlot *slot, int tile, unsigned 
     const GraphPair &gp = a.graphs[d.gidx];
     const DGraph &gx = d.side ? gp.rev : gp.fwd;
     AppendTarget app{d.log, d.cap, d.side, &slot->tc.tail[d.side], &slot->tc.deg[d.side],
-                     gx.row_ptr};
+                     gx.row_ptr, d.track_hist ? slot->tc.hist[d.side] : nullptr};
     if (tile >= d.nvt) {
         // row job: wait (bounded) until its descriptor carries this step's seq
         RowJob *J = a.jobs + (size_t)(slot - a.slots) * POOL_JOBS + (tile - d.nvt);
@@ -193,20 +195,24 @@ __device__ void pool_tile(const PoolArgs &a, PoolSlot *slot, int tile, unsigned 
         return;
     }
     if (d.dir == DIR_TD) {
-        const int i = tile * T + tid;
-        int rb = 0, re = 0;
-        if (i < d.F) {
-            int u = ld_cg(d.log + d.front_off + i);
-            rb = __ldg(gx.row_ptr + u);
-            re = __ldg(gx.row_ptr + u + 1);
-        }
         SlotSink sink{slot, a.jobs + (size_t)(slot - a.slots) * POOL_JOBS, seq};
-        if (d.mode == MODE_BFS) {
-            VisitBFS vis{d.levels, d.level + 1};
-            pool_expand<T>(d.variant, gx.col, rb, re, vis, app, sm.td, sink);
-        } else {
-            VisitSTCON vis{d.status, st_code(d.side, d.level + 1), d.side, &slot->tc.found};
-            pool_expand<T>(d.variant, gx.col, rb, re, vis, app, sm.td, sink);
+        for (int c = 0; c < d.tile_mult; ++c) {
+            const long long base = ((long long)tile * d.tile_mult + c) * T;
+            if (base >= d.F) break;  // uniform: same for every thread
+            const long long i = base + tid;
+            int rb = 0, re = 0;
+            if (i < d.F) {
+                int u = ld_cg(d.log + d.front_off + i);
+                rb = __ldg(gx.row_ptr + u);
+                re = __ldg(gx.row_ptr + u + 1);
+            }
+            if (d.mode == MODE_BFS) {
+                VisitBFS vis{d.levels, d.level + 1};
+                pool_expand<T>(d.variant, gx.col, rb, re, vis, app, sm.td, sink);
+            } else {
+                VisitSTCON vis{d.status, st_code(d.side, d.level + 1), d.side, &slot->tc.found};
+                pool_expand<T>(d.variant, gx.col, rb, re, vis, app, sm.td, sink);
+            }
         }
         return;
     }
@@ -399,17 +405,43 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
     desc.levels = levels;
     desc.log = log;
     desc.nreset = 0;
+    // the degree histogram is counted only for the learned schedule and traces
+    const bool track = (a.sched == FC_SCHED_LEARNED && a.mlp) || a.trace;
+    desc.track_hist = track;
+    const int bu_cap = a.mode == MODE_BFS ? INT_MAX : LEVEL7_MAX;
     while (true) {
-        if (tid == 0 && !sm.ql.done) {
-            ql_decide(sm.ql, a.sched, 1, a.mode == MODE_BFS ? INT_MAX : LEVEL7_MAX, 1,
-                      a.force_variant);
-            const int x = sm.ql.side;
-            const long long m = (long long)(sm.ql.dt[x] - sm.ql.dh[x]);
-            if (!a.exclusive && (long long)sm.ql.tail[0] + sm.ql.tail[1] + m > cap) {
-                sm.ql.escalate = 1;  // the log could overflow: finish it in exclusive mode
-                sm.ql.done = 1;
+        if (tid < 32 && !sm.ql.done) {
+            // warp 0 decides: policy, then the MLP (warp-level), then a script
+            if (tid == 0) ql_decide(sm.ql, a.sched, 1, bu_cap, 1, a.force_variant);
+            __syncwarp();
+            if (track) {
+                float f[MLP_IN];
+                ql_features(sm.ql, f);
+                if (a.sched == FC_SCHED_LEARNED && a.mlp) {
+                    float o[MLP_OUT];
+                    mlp_forward_warp(a.mlp, f, o);
+                    if (tid == 0) {
+                        ql_apply_logits(sm.ql, o, 1, bu_cap);
+                        if (a.force_variant >= 0) sm.ql.variant = a.force_variant;
+                    }
+                }
+                if (tid == 0)
+                    for (int i = 0; i < MLP_IN; ++i) sm.ql.feat[i] = f[i];
             }
-            sm.publish = sm.ql.dir == DIR_BU || m > a.private_edges;
+            if (tid == 0) {
+                if (a.script && sm.ql.steps < a.script_len) {
+                    const unsigned char act = a.script[(size_t)q * a.script_len + sm.ql.steps];
+                    if (act != 0xFF) ql_apply_script(sm.ql, act, 1, bu_cap);
+                }
+                const int x = sm.ql.side;
+                const long long m = (long long)(sm.ql.dt[x] - sm.ql.dh[x]);
+                if (!a.exclusive && (long long)sm.ql.tail[0] + sm.ql.tail[1] + m > cap) {
+                    sm.ql.escalate = 1;  // the log could overflow: finish it in exclusive mode
+                    sm.ql.done = 1;
+                }
+                sm.publish = sm.ql.dir == DIR_BU || m > a.private_edges;
+                sm.t_step = global_timer_ns();
+            }
         }
         __syncthreads();
         if (sm.ql.done) break;
@@ -419,7 +451,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
         if (!sm.publish) {
             run_step<T>(a.mode, gp, x, DIR_TD, sm.ql.radius[x], sm.ql.radius[1 - x], front, F, 0, 1,
                         status, levels, log, cap, &my->tc.tail[x], &my->tc.deg[x], &my->tc.found,
-                        &my->tc.inspected, sm.td, sm.ql.variant);
+                        &my->tc.inspected, sm.td, sm.ql.variant, track ? my->tc.hist[x] : nullptr);
             __syncthreads();
         } else {
             desc.side = x;
@@ -429,14 +461,49 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             desc.other_radius = sm.ql.radius[1 - x];
             desc.F = F;
             desc.front_off = (int)(front - log);
-            const int nvt = desc.dir == DIR_TD ? (F + T - 1) / T : (nv + POOL_TILE_V - 1) / POOL_TILE_V;
+            // about 8 tiles per CTA at most: fewer claims on the slot word
+            const int chunks = (F + T - 1) / T;
+            const int want = 8 * (int)gridDim.x;
+            desc.tile_mult = chunks > want ? (chunks + want - 1) / want : 1;
+            const int nvt = desc.dir == DIR_TD ? (chunks + desc.tile_mult - 1) / desc.tile_mult
+                                               : (nv + POOL_TILE_V - 1) / POOL_TILE_V;
             desc.nvt = nvt;
             pool_publish_and_run<T>(a, my, desc, nvt, sm);
             if (sm.err) return;
         }
-        if (tid == 0)
+        if (tid == 0) {
+            const unsigned long long ins0 = sm.ql.inspected;
+            const int tail0 = sm.ql.tail[x], F0 = sm.ql.tail[x] - sm.ql.head[x];
+            const int dir0 = sm.ql.dir, var0 = sm.ql.variant, step0 = sm.ql.steps;
             ql_update(sm.ql, ld_cg(&my->tc.found), ld_cg(&my->tc.tail[x]), ld_cg_u64(&my->tc.deg[x]),
                       ld_cg_u64(&my->tc.inspected));
+            if (track) {
+                unsigned long long h3[3];
+                for (int b = 0; b < 3; ++b) h3[b] = ld_cg_u64(&my->tc.hist[x][b]);
+                ql_update_hist(sm.ql, x, h3);
+            }
+            if (a.trace) {
+                const int k = atomicAdd(a.trace_count, 1);
+                if (k < a.trace_cap) {
+                    int32_t *r = a.trace + (size_t)k * TRACE_WORDS;
+                    const unsigned long long cost = sm.ql.inspected - ins0;
+                    const unsigned long long dt = global_timer_ns() - sm.t_step;
+                    r[0] = q;
+                    r[1] = step0;
+                    r[2] = x;
+                    r[3] = dir0;
+                    r[4] = var0;
+                    r[5] = sm.ql.connected && sm.ql.done;
+                    r[6] = (int32_t)(cost & 0xFFFFFFFFull);
+                    r[7] = (int32_t)(cost >> 32);
+                    r[8] = (int32_t)(dt & 0xFFFFFFFFull);
+                    r[9] = (int32_t)(dt >> 32);
+                    r[10] = sm.ql.tail[x] - tail0;
+                    r[11] = F0;
+                    for (int i = 0; i < MLP_IN; ++i) r[12 + i] = __float_as_int(sm.ql.feat[i]);
+                }
+            }
+        }
         __syncthreads();
     }
     if (tid == 0) {
@@ -445,6 +512,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             a.spill[k] = q;
         }
         write_result(q, sm.ql, a.out_conn, a.out_hops, a.qstat, sm.ql.escalate);
+        if (a.out_inspected && !sm.ql.escalate) a.out_inspected[q] = (long long)sm.ql.inspected;
     }
     // clear exactly the claimed status bytes (s-t mode), sharing big resets
     if (a.mode == MODE_STCON) {

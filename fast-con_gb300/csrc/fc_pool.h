@@ -36,7 +36,21 @@ struct PoolArgs {
     int32_t *out_conn;
     int32_t *out_hops;
     QueryStat *qstat;
+    // learned schedule and its training data
+    const float *mlp;                 // MLP weights (nullable: the heuristic decides)
+    const unsigned char *script;      // per query script_len action bytes (nullable)
+    int script_len;
+    int32_t *trace;                   // TRACE_WORDS ints per step record (nullable)
+    int trace_cap;
+    int *trace_count;
+    long long *out_inspected;         // per-query adjacency entries read (nullable)
 };
+
+// One trace record per executed step (ints; features are float bit patterns):
+// [0] query [1] step [2] side [3] direction [4] variant [5] met in this step
+// [6,7] entries read by the step (lo, hi) [8,9] owner-measured ns (lo, hi)
+// [10] vertices claimed [11] frontier vertices [12..23] the 12 features
+constexpr int TRACE_WORDS = 24;
 
 size_t pool_slot_bytes();
 size_t pool_job_bytes();  // per slot

@@ -16,7 +16,11 @@ struct TeamCounters {
     int bar[2];
     int invalid;
     int pad;
+    unsigned long long hist[2][3];  // claimed vertices per side by degree bin (learned schedule)
 };
+
+// degree bins of the frontier histogram: < 8, < 128, >= 128
+__host__ __device__ inline int deg_bin(long long d) { return d < 8 ? 0 : (d < 128 ? 1 : 2); }
 
 struct GraphPair {
     DGraph fwd, rev;
@@ -42,11 +46,19 @@ struct QLocal {
     int two;
     int nv;
     long long ne;
+    unsigned long long hh[2][3], ht[2][3];  // histogram counters at head / tail
+    int last_side;
+    float feat[12];                          // features of the last decision
 };
 
 __host__ __device__ inline void ql_start(QLocal &q, int two, int nv, long long ne, int s, int t,
                                          unsigned long long deg_s, unsigned long long deg_t)
 {
+    for (int x = 0; x < 2; ++x)
+        for (int b = 0; b < 3; ++b) q.hh[x][b] = q.ht[x][b] = 0;
+    q.ht[0][deg_bin((long long)deg_s)] = 1;
+    if (two && s != t) q.ht[1][deg_bin((long long)deg_t)] = 1;
+    q.last_side = -1;
     q.head[0] = q.head[1] = 0;
     q.tail[0] = 1;
     q.tail[1] = (two && s != t) ? 1 : 0;
@@ -101,12 +113,13 @@ __host__ __device__ inline void ql_decide(QLocal &q, int sched, int allow_bu, in
     q.dir = DIR_TD;
     q.variant = VAR_HYBRID;
     if (sched != FC_SCHED_PLAIN) {
+        // low average degree: one lane per row; otherwise the CTA hybrid,
+        // which measured fastest on R-MAT frontiers in every engine (the
+        // warp-centric variant is left to the learned schedule)
         const long long nf = q.tail[side] - q.head[side];
         const long long mf = (long long)(q.dt[side] - q.dh[side]);
-        if (mf < 8 * nf)
-            q.variant = VAR_THREAD;  // low, even degrees: one lane per row
-        else if (long_rows_split)
-            q.variant = VAR_WARP;
+        if (mf < 8 * nf) q.variant = VAR_THREAD;
+        (void)long_rows_split;
     }
     if (sched != FC_SCHED_PLAIN && allow_bu && q.radius[side] + 1 <= bu_level_cap) {
         long long mf = (long long)(q.dt[side] - q.dh[side]);
@@ -141,6 +154,7 @@ __host__ __device__ inline void ql_update(QLocal &q, int found, int tail_x,
     }
     q.bu_seen = bu_total;
     q.steps++;
+    q.last_side = x;
     if (found && q.two) {
         q.done = 1;
         q.connected = 1;
@@ -156,6 +170,124 @@ __host__ __device__ inline void ql_update(QLocal &q, int found, int tail_x,
         q.connected = 0;
         q.hops = -1;
     }
+}
+
+// After ql_update for side x: move the side's histogram window forward.
+__host__ __device__ inline void ql_update_hist(QLocal &q, int x, const unsigned long long *h3)
+{
+    for (int b = 0; b < 3; ++b) {
+        q.hh[x][b] = q.ht[x][b];
+        q.ht[x][b] = h3[b];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Learned schedule.  Twelve features per decision (all from integer counters):
+//   0,1  log2(1 + frontier vertices) / 24 of side 0, side 1
+//   2,3  log2(1 + frontier adjacency entries) / 32 of side 0, side 1
+//   4    unexplored fraction: adjacency entries of unclaimed vertices / ne
+//   5    side expanded last (0 or 1; 0.5 before the first step)
+//   6-8  side 0 frontier degree histogram (< 8, < 128, >= 128), fractions
+//   9-11 side 1 frontier degree histogram, fractions
+// MLP 12 -> 32 (ReLU) -> 32 (ReLU) -> 7 logits: side (2), direction (2),
+// expansion variant (3).  1,703 float parameters in this order:
+//   W1[32][12], b1[32], W2[32][32], b2[32], W3[7][32], b3[7].
+// ---------------------------------------------------------------------------
+constexpr int MLP_IN = 12, MLP_H = 32, MLP_OUT = 7;
+constexpr int MLP_W1 = 0, MLP_B1 = MLP_W1 + MLP_H * MLP_IN, MLP_W2 = MLP_B1 + MLP_H,
+              MLP_B2 = MLP_W2 + MLP_H * MLP_H, MLP_W3 = MLP_B2 + MLP_H,
+              MLP_B3 = MLP_W3 + MLP_OUT * MLP_H, MLP_PARAMS = MLP_B3 + MLP_OUT;
+static_assert(MLP_PARAMS == 1703, "parameter count");
+
+__host__ __device__ inline void ql_features(const QLocal &q, float *f)
+{
+    const double n0 = (double)(q.tail[0] - q.head[0]), n1 = (double)(q.tail[1] - q.head[1]);
+    const double m0 = (double)(q.dt[0] - q.dh[0]), m1 = (double)(q.dt[1] - q.dh[1]);
+    long long un = q.ne - (long long)(q.dt[0] + q.dt[1]);
+    if (un < 0) un = 0;
+    f[0] = (float)(log2(1.0 + n0) / 24.0);
+    f[1] = (float)(log2(1.0 + n1) / 24.0);
+    f[2] = (float)(log2(1.0 + m0) / 32.0);
+    f[3] = (float)(log2(1.0 + m1) / 32.0);
+    f[4] = q.ne > 0 ? (float)((double)un / (double)q.ne) : 0.f;
+    f[5] = q.last_side < 0 ? 0.5f : (float)q.last_side;
+    for (int x = 0; x < 2; ++x) {
+        double h[3], tot = 0;
+        for (int b = 0; b < 3; ++b) {
+            h[b] = (double)(q.ht[x][b] - q.hh[x][b]);
+            tot += h[b];
+        }
+        for (int b = 0; b < 3; ++b) f[6 + 3 * x + b] = tot > 0 ? (float)(h[b] / tot) : 0.f;
+    }
+}
+
+// Forward pass by one thread (host-loop engine on the host, grid engine on
+// the device).
+__host__ __device__ inline void mlp_forward_scalar(const float *W, const float *f, float *out)
+{
+    float h1[MLP_H], h2[MLP_H];
+    for (int j = 0; j < MLP_H; ++j) {
+        float a = W[MLP_B1 + j];
+        for (int i = 0; i < MLP_IN; ++i) a += W[MLP_W1 + j * MLP_IN + i] * f[i];
+        h1[j] = a > 0.f ? a : 0.f;
+    }
+    for (int j = 0; j < MLP_H; ++j) {
+        float a = W[MLP_B2 + j];
+        for (int k = 0; k < MLP_H; ++k) a += W[MLP_W2 + j * MLP_H + k] * h1[k];
+        h2[j] = a > 0.f ? a : 0.f;
+    }
+    for (int o = 0; o < MLP_OUT; ++o) {
+        float a = W[MLP_B3 + o];
+        for (int k = 0; k < MLP_H; ++k) a += W[MLP_W3 + o * MLP_H + k] * h2[k];
+        out[o] = a;
+    }
+}
+
+// Forward pass by one warp: lane j computes hidden unit j of both layers; the
+// 7 outputs are warp reductions.  Every lane returns all 7 logits.
+__device__ __forceinline__ void mlp_forward_warp(const float *__restrict__ W, const float *f,
+                                                 float *out)
+{
+    const int j = (int)lane_id();
+    float a = __ldg(W + MLP_B1 + j);
+#pragma unroll
+    for (int i = 0; i < MLP_IN; ++i) a += __ldg(W + MLP_W1 + j * MLP_IN + i) * f[i];
+    const float h1 = a > 0.f ? a : 0.f;
+    a = __ldg(W + MLP_B2 + j);
+#pragma unroll 8
+    for (int k = 0; k < MLP_H; ++k) a += __ldg(W + MLP_W2 + j * MLP_H + k) * __shfl_sync(0xffffffffu, h1, k);
+    const float h2 = a > 0.f ? a : 0.f;
+#pragma unroll
+    for (int o = 0; o < MLP_OUT; ++o) {
+        float v = __ldg(W + MLP_W3 + o * MLP_H + j) * h2;
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+        out[o] = v + __ldg(W + MLP_B3 + o);
+    }
+}
+
+// Turn logits (or a scripted action) into the step, within the engine's
+// constraints: one side only for BFS, bottom-up only where allowed.
+__host__ __device__ inline void ql_apply_logits(QLocal &q, const float *o, int allow_bu,
+                                                int bu_level_cap)
+{
+    q.side = q.two ? (o[1] > o[0] ? 1 : 0) : 0;
+    q.dir = (allow_bu && q.radius[q.side] + 1 <= bu_level_cap && o[3] > o[2]) ? DIR_BU : DIR_TD;
+    int v = 0;
+    if (o[5] > o[4 + v]) v = 1;
+    if (o[6] > o[4 + v]) v = 2;
+    q.variant = v;
+}
+
+// Scripted action byte: bit 0 side, bit 1 bottom-up, bits 2-3 variant + 1
+// (0 = the schedule's variant); 0xFF = no script for this step.
+__host__ __device__ inline void ql_apply_script(QLocal &q, unsigned char a, int allow_bu,
+                                                int bu_level_cap)
+{
+    q.side = q.two ? (a & 1) : 0;
+    q.dir = ((a >> 1) & 1) && allow_bu && q.radius[q.side] + 1 <= bu_level_cap ? DIR_BU : DIR_TD;
+    const int v = (a >> 2) & 3;
+    if (v) q.variant = v - 1;
 }
 
 __device__ __forceinline__ const int32_t *ql_frontier(const QLocal &q, const int32_t *log, int cap,
@@ -190,10 +322,11 @@ __device__ void run_step(int mode, const GraphPair &gp, int side, int dir, int l
                          int other_radius, const int32_t *frontier, int F, int team_rank,
                          int team_size, uint8_t *status, int32_t *levels, int32_t *log, int cap,
                          int *tail_ctr, unsigned long long *deg_ctr, int *found,
-                         unsigned long long *bu_ins, SmemTopDown<T> &sm, int variant = VAR_HYBRID)
+                         unsigned long long *bu_ins, SmemTopDown<T> &sm, int variant = VAR_HYBRID,
+                         unsigned long long *hist = nullptr)
 {
     const DGraph &gx = side ? gp.rev : gp.fwd;
-    AppendTarget app{log, cap, side, tail_ctr, deg_ctr, gx.row_ptr};
+    AppendTarget app{log, cap, side, tail_ctr, deg_ctr, gx.row_ptr, hist};
     if (dir == DIR_TD) {
         if (mode == MODE_BFS) {
             VisitBFS vis{levels, level + 1};
@@ -224,6 +357,8 @@ __device__ inline void init_roots(int mode, const GraphPair &gp, int s, int t, u
     tc->found = 0;
     tc->inspected = 0;
     tc->invalid = 0;
+    for (int x = 0; x < 2; ++x)
+        for (int b = 0; b < 3; ++b) tc->hist[x][b] = 0;
     if (mode == MODE_BFS) {
         levels[s] = 0;
         log[0] = s;
@@ -231,8 +366,11 @@ __device__ inline void init_roots(int mode, const GraphPair &gp, int s, int t, u
         tc->tail[1] = 0;
         tc->deg[0] = (unsigned long long)(gp.fwd.row_ptr[s + 1] - gp.fwd.row_ptr[s]);
         tc->deg[1] = 0;
+        tc->hist[0][deg_bin((long long)tc->deg[0])] = 1;
         return;
     }
+    tc->hist[0][deg_bin((long long)(gp.fwd.row_ptr[s + 1] - gp.fwd.row_ptr[s]))] = 1;
+    if (s != t) tc->hist[1][deg_bin((long long)(gp.rev.row_ptr[t + 1] - gp.rev.row_ptr[t]))] = 1;
     status[s] = st_code(0, 0);
     log[0] = s;
     tc->tail[0] = 1;

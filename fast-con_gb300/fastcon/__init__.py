@@ -37,7 +37,8 @@ EXPORTS = [
     "fc_graph_from_device_edges", "fc_graph_generate_rmat", "fc_graph_generate_grid",
     "fc_graph_info", "fc_graph_get_csr", "fc_graph_free", "fc_bfs_levels", "fc_bfs_levels_ex",
     "fc_stcon", "fc_stcon_ex", "fc_stcon_depth", "fc_stcon_batch", "fc_stcon_batch_device",
-    "fc_stcon_batch_noalloc",
+    "fc_stcon_batch_noalloc", "fc_sched_set_weights", "fc_sched_get_weights",
+    "fc_mlp_loss_grad", "fc_mlp_train", "fc_stcon_batch_scripted",
     "fc_strerror", "fc_last_error_message", "fc_device_info", "fc_version",
 ]
 
@@ -106,6 +107,12 @@ def lib():
             "fc_stcon_batch_device": (ctypes.c_int, [_VP, _I32, _VP, _VP, _VP, _I32, _VP, _VP, _VP, _VP]),
             "fc_stcon_batch_noalloc": (ctypes.c_int, [_VP, _VP, _I32, _I64, _VP, _VP, _VP, _VP,
                                                       _I32, _VP, _VP, _I32, _VP]),
+            "fc_sched_set_weights": (ctypes.c_int, [_VP, _I32]),
+            "fc_sched_get_weights": (ctypes.c_int, [_VP, _I32]),
+            "fc_mlp_loss_grad": (ctypes.c_int, [_VP, _VP, _I32, _VP, _VP, _VP]),
+            "fc_mlp_train": (ctypes.c_int, [_VP, _VP, _I32, _I32, _I32, ctypes.c_float, _VP, _VP]),
+            "fc_stcon_batch_scripted": (ctypes.c_int, [_VP, _VP, _VP, _I32, _VP, _I32, _VP, _VP,
+                                                       _VP, _VP, _I32, _VP]),
             "fc_strerror": (ctypes.c_char_p, [ctypes.c_int]),
             "fc_last_error_message": (ctypes.c_char_p, []),
             "fc_device_info": (ctypes.c_int, [_VP, _VP, _VP, _VP]),

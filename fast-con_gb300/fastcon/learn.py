@@ -1,0 +1,332 @@
+"""Learned schedule: training data, GPU training, evaluation.
+
+    python -m fastcon.learn [--queries 20000] [--out fastcon/sched_weights.json]
+
+1. Graphs: R-MAT scale 18-22 (a/b/c/d = .57/.19/.19/.05, 8 * 2^scale edge
+   samples, ids permuted), seeds 1000 + i.
+2. Traces: every query runs once under the plain schedule and once under the
+   heuristic schedule with step tracing on (fc_stcon_batch_scripted); each
+   traced step is a state with 12 features and the action taken.
+3. Side / direction labels: at each sampled state the query is re-run with a
+   script that replays the trace's earlier actions and forces one of the four
+   (side, direction) actions at that step, after which the heuristic finishes
+   the query.  The action with the fewest adjacency entries read in total is
+   the label (ties keep the earlier candidate: top-down, side of s first).
+4. Variant labels: the trace's actions are replayed with each expansion
+   variant forced; the variant whose step took the least time is the label.
+5. Training: fc_mlp_train (the library's CUDA forward/backward/Adam kernels).
+6. Evaluation: held-out graphs, edges inspected / time / exactness per schedule.
+
+Device buffers for the library's device-array calls come from torch.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import time
+
+import numpy as np
+
+from . import (ENGINE_BATCHED, SCHED_HEURISTIC, SCHED_LEARNED, SCHED_PLAIN, Graph, _check, lib,
+               make_opts, stcon_batch)
+from . import graphs
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+WEIGHTS_PATH = os.path.join(HERE, "sched_weights.json")
+N_PARAMS = 1703
+TRACE_WORDS = 24
+CANDIDATES = [(0, 0), (1, 0), (0, 1), (1, 1)]  # (side, bottom-up)
+
+
+def init_weights(seed: int = 0) -> np.ndarray:
+    """He-uniform initialisation of the 12-32-32-7 network (float32)."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for fan_in, fan_out in ((12, 32), (32, 32), (32, 7)):
+        lim = np.sqrt(6.0 / fan_in)
+        parts.append(rng.uniform(-lim, lim, size=(fan_out, fan_in)).ravel())
+        parts.append(np.zeros(fan_out))
+    w = np.concatenate(parts).astype(np.float32)
+    assert w.size == N_PARAMS
+    return w
+
+
+def set_weights(w: np.ndarray) -> None:
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    _check(lib().fc_sched_set_weights(ctypes.c_void_p(w.ctypes.data), w.size),
+           "fc_sched_set_weights")
+
+
+def load_default_weights(path: str = WEIGHTS_PATH) -> dict:
+    d = json.load(open(path))
+    set_weights(np.array(d["weights"], dtype=np.float32))
+    return d
+
+
+def loss_grad(X: np.ndarray, Y: np.ndarray, w: np.ndarray):
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    Y = np.ascontiguousarray(Y, dtype=np.int32)
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    g = np.zeros(N_PARAMS, np.float32)
+    loss = np.zeros(1, np.float32)
+    _check(lib().fc_mlp_loss_grad(X.ctypes.data, Y.ctypes.data, len(X), w.ctypes.data,
+                                  g.ctypes.data, loss.ctypes.data), "fc_mlp_loss_grad")
+    return float(loss[0]), g
+
+
+def train(X, Y, epochs=40, batch=256, lr=3e-3, seed=0, w0=None):
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    Y = np.ascontiguousarray(Y, dtype=np.int32)
+    w = init_weights(seed) if w0 is None else np.array(w0, dtype=np.float32)
+    curve = np.zeros(epochs, np.float32)
+    _check(lib().fc_mlp_train(X.ctypes.data, Y.ctypes.data, len(X), epochs, batch,
+                              ctypes.c_float(lr), w.ctypes.data, curve.ctypes.data),
+           "fc_mlp_train")
+    return w, curve
+
+
+# ---------------------------------------------------------------------------
+# scripted / traced runs
+# ---------------------------------------------------------------------------
+def run_scripted(G: Graph, s, t, script=None, sched=SCHED_HEURISTIC, variant=0, trace=False,
+                 cta_work_k=0):
+    """Returns (hops, inspected per query, trace records [k, 24] or None)."""
+    import torch
+    nq = len(s)
+    d_s = torch.from_numpy(np.ascontiguousarray(s, dtype=np.int32)).cuda()
+    d_t = torch.from_numpy(np.ascontiguousarray(t, dtype=np.int32)).cuda()
+    d_h = torch.empty(nq, dtype=torch.int32, device="cuda")
+    d_i = torch.empty(nq, dtype=torch.int64, device="cuda")
+    d_sc, L = None, 0
+    if script is not None:
+        script = np.ascontiguousarray(script, dtype=np.uint8)
+        L = script.shape[1]
+        d_sc = torch.from_numpy(script.ravel()).cuda()
+    cap = 64 * nq if trace else 0
+    d_tr = torch.empty(max(1, cap) * TRACE_WORDS, dtype=torch.int32, device="cuda") if trace else None
+    d_tc = torch.zeros(1, dtype=torch.int32, device="cuda") if trace else None
+    o = make_opts(sched=sched, engine=ENGINE_BATCHED, variant=variant, cta_work_k=cta_work_k)
+    torch.cuda.synchronize()
+    _check(lib().fc_stcon_batch_scripted(
+        G.handle, d_s.data_ptr(), d_t.data_ptr(), nq, d_sc.data_ptr() if d_sc is not None else None,
+        L, ctypes.byref(o), d_h.data_ptr(), d_i.data_ptr(),
+        d_tr.data_ptr() if trace else None, cap, d_tc.data_ptr() if trace else None),
+        "fc_stcon_batch_scripted")
+    recs = None
+    if trace:
+        k = min(int(d_tc.item()), cap)
+        recs = d_tr[: k * TRACE_WORDS].view(k, TRACE_WORDS).cpu().numpy()
+    return d_h.cpu().numpy(), d_i.cpu().numpy(), recs
+
+
+def decode(recs: np.ndarray):
+    """Trace records -> dict of arrays."""
+    r = recs
+    return {
+        "q": r[:, 0], "step": r[:, 1], "side": r[:, 2], "dir": r[:, 3], "variant": r[:, 4],
+        "met": r[:, 5],
+        "cost": r[:, 6].astype(np.uint32).astype(np.int64) + (r[:, 7].astype(np.int64) << 32),
+        "ns": r[:, 8].astype(np.uint32).astype(np.int64) + (r[:, 9].astype(np.int64) << 32),
+        "claimed": r[:, 10], "frontier": r[:, 11],
+        "feat": np.ascontiguousarray(r[:, 12:24]).view(np.float32),
+    }
+
+
+def action_byte(side, bu, variant=-1):
+    return int(side) | (int(bu) << 1) | ((int(variant) + 1) << 2 if variant >= 0 else 0)
+
+
+def trace_actions(tr, nq):
+    """Per query: list of (step, side, dir) in step order."""
+    order = np.lexsort((tr["step"], tr["q"]))
+    acts = [[] for _ in range(nq)]
+    for i in order:
+        acts[tr["q"][i]].append((int(tr["step"][i]), int(tr["side"][i]), int(tr["dir"][i]), i))
+    return acts
+
+
+def label_states(G: Graph, s, t, tr, max_states: int, rng):
+    """Side/direction labels by scripted rollouts at sampled trace states."""
+    nq = len(s)
+    acts = trace_actions(tr, nq)
+    states = [(q, k) for q in range(nq) for k in range(len(acts[q]))]
+    if len(states) > max_states:
+        pick = rng.choice(len(states), size=max_states, replace=False)
+        states = [states[i] for i in sorted(pick)]
+    if not states:
+        return np.zeros((0, 12), np.float32), np.zeros((0, 3), np.int32), []
+    L = max(k for _, k in states) + 1
+    rs, rt, scripts = [], [], []
+    for q, k in states:
+        prefix = [action_byte(a[1], a[2]) for a in acts[q][:k]]
+        for side, bu in CANDIDATES:
+            sc = np.full(L, 0xFF, np.uint8)
+            sc[:k] = prefix
+            sc[k] = action_byte(side, bu)
+            scripts.append(sc)
+            rs.append(s[q])
+            rt.append(t[q])
+    hops, ins, _ = run_scripted(G, np.array(rs), np.array(rt), np.stack(scripts),
+                                sched=SCHED_HEURISTIC)
+    ins = ins.reshape(len(states), len(CANDIDATES))
+    best = np.argmin(ins, axis=1)  # argmin keeps the first minimum
+    X = np.stack([tr["feat"][acts[q][k][3]] for q, k in states]).astype(np.float32)
+    Y = np.full((len(states), 3), -1, np.int32)
+    Y[:, 0] = [CANDIDATES[b][0] for b in best]
+    Y[:, 1] = [CANDIDATES[b][1] for b in best]
+    return X, Y, [(q, k) for q, k in states]
+
+
+def label_variants(G: Graph, s, t, tr, states):
+    """Variant label per state: fastest step when the trace is replayed with
+    each variant forced."""
+    nq = len(s)
+    acts = trace_actions(tr, nq)
+    L = max(1, max(len(a) for a in acts))
+    script = np.full((nq, L), 0xFF, np.uint8)
+    for q in range(nq):
+        for k, (_, side, d, _) in enumerate(acts[q]):
+            script[q, k] = action_byte(side, d)
+    times = []
+    for v in (1, 2, 3):
+        _, _, rec = run_scripted(G, s, t, script, sched=SCHED_HEURISTIC, variant=v, trace=True)
+        d = decode(rec)
+        tm = {}
+        for i in range(len(d["q"])):
+            tm[(int(d["q"][i]), int(d["step"][i]))] = int(d["ns"][i])
+        times.append(tm)
+    lab = []
+    for q, k in states:
+        ts = [tm.get((q, k), 1 << 62) for tm in times]
+        lab.append(int(np.argmin(ts)))
+    return np.array(lab, np.int32)
+
+
+def build_dataset(total_queries=20000, scales=(18, 19, 20, 21, 22), first_seed=1000,
+                  states_per_graph=6000, seed=0, log=print):
+    rng = np.random.default_rng(seed)
+    per_graph = total_queries // (2 * len(scales))
+    Xs, Ys = [], []
+    gi = 0
+    for rep in range(2):
+        for sc in scales:
+            gseed = first_seed + gi
+            gi += 1
+            G = Graph.rmat(sc, 8 << sc, seed=gseed, perm_seed=gseed)
+            rp, _ = G.csr_row_ptr()
+            s, t = graphs.pairs_with_degree(np.diff(rp), per_graph, seed=gseed + 500)
+            for pol in (SCHED_PLAIN, SCHED_HEURISTIC):
+                _, _, rec = run_scripted(G, s, t, None, sched=pol, trace=True)
+                tr = decode(rec)
+                X, Y, states = label_states(G, s, t, tr, states_per_graph // 2, rng)
+                Y[:, 2] = label_variants(G, s, t, tr, states)
+                Xs.append(X)
+                Ys.append(Y)
+                log(f"graph scale {sc} seed {gseed} policy {pol}: {len(X)} states, "
+                    f"labels side1 {Y[:, 0].mean():.2f} bu {Y[:, 1].mean():.2f} "
+                    f"variant {np.bincount(Y[:, 2], minlength=3).tolist()}")
+            G.free()
+    X = np.concatenate(Xs)
+    Y = np.concatenate(Ys)
+    perm = rng.permutation(len(X))
+    return X[perm], Y[perm]
+
+
+# ---------------------------------------------------------------------------
+# evaluation
+# ---------------------------------------------------------------------------
+def evaluate(G: Graph, s, t, want_hops=None, reps=3):
+    out = {}
+    for name, sched in (("plain", SCHED_PLAIN), ("heuristic", SCHED_HEURISTIC),
+                        ("learned", SCHED_LEARNED)):
+        o = make_opts(sched=sched, engine=ENGINE_BATCHED)
+        best = None
+        for _ in range(reps):
+            conn, hops, st = stcon_batch(G, s, t, opts=o, stats=True)
+            ms = st["kernel_ms"][0] + st["kernel_ms"][1]
+            best = ms if best is None else min(best, ms)
+        r = {"edges_inspected": int(st["edges_inspected"]), "gpu_ms": best,
+             "queries_per_s": len(s) / (best / 1000.0), "bottom_up_steps": st["bottom_up_steps"],
+             "steps": st["steps"]}
+        if want_hops is not None:
+            r["exact"] = bool((hops == want_hops).all())
+        out[name] = r
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--queries", type=int, default=20000)
+    ap.add_argument("--epochs", type=int, default=60)
+    ap.add_argument("--out", default=WEIGHTS_PATH)
+    ap.add_argument("--eval-queries", type=int, default=4096)
+    args = ap.parse_args()
+    t0 = time.time()
+    X, Y = build_dataset(args.queries)
+    t1 = time.time()
+    nval = len(X) // 10
+    w, curve = train(X[nval:], Y[nval:], epochs=args.epochs)
+    vloss, _ = loss_grad(X[:nval], Y[:nval], w)
+    # validation accuracy per head (host forward pass in float64)
+    acc = head_accuracy(X[:nval], Y[:nval], w)
+    t2 = time.time()
+    set_weights(w)
+    ev = {}
+    G = Graph.rmat(24, 8 << 24, seed=9, perm_seed=9)
+    rp, _ = G.csr_row_ptr()
+    s, t = graphs.pairs_with_degree(np.diff(rp), args.eval_queries, seed=9)
+    ref = stcon_batch(G, s, t, opts=make_opts(sched=SCHED_PLAIN, engine=ENGINE_BATCHED))[1]
+    ev["rmat24_seed9"] = evaluate(G, s, t, ref)
+    G.free()
+    n = 4096 * 4096
+    G = Graph.grid(4096, 4096, p_del=0.05, del_seed=5, shortcuts=graphs.grid_shortcut_count(n),
+                   sc_seed=6)
+    s, t = graphs.grid_pairs(4096, 4096, args.eval_queries, 17, 2000)
+    ref = stcon_batch(G, s, t, opts=make_opts(sched=SCHED_PLAIN, engine=ENGINE_BATCHED))[1]
+    ev["grid4096"] = evaluate(G, s, t, ref)
+    G.free()
+    meta = {
+        "weights": [float(x) for x in w],
+        "layout": "W1[32][12] b1[32] W2[32][32] b2[32] W3[7][32] b3[7]",
+        "training": {"graphs": "R-MAT scale 18-22 x2, seeds 1000-1009", "queries": args.queries,
+                     "samples": int(len(X) - nval), "validation": int(nval),
+                     "epochs": args.epochs, "loss_curve": [float(x) for x in curve],
+                     "validation_loss": vloss, "validation_accuracy": acc,
+                     "label_balance": {"side1": float(Y[:, 0].mean()), "bottom_up": float(Y[:, 1].mean()),
+                                       "variant": np.bincount(Y[:, 2], minlength=3).tolist()},
+                     "seconds": {"dataset": t1 - t0, "train": t2 - t1}},
+        "evaluation": ev,
+    }
+    with open(args.out, "w") as f:
+        json.dump(meta, f, indent=1)
+    print(json.dumps({k: v for k, v in meta.items() if k != "weights"}, indent=1))
+
+
+def forward_np(X, w):
+    """float64 restatement of the network (also used by the gradient test)."""
+    w = np.asarray(w, np.float64)
+    W1 = w[0:384].reshape(32, 12)
+    b1 = w[384:416]
+    W2 = w[416:1440].reshape(32, 32)
+    b2 = w[1440:1472]
+    W3 = w[1472:1696].reshape(7, 32)
+    b3 = w[1696:1703]
+    h1 = np.maximum(X @ W1.T + b1, 0)
+    h2 = np.maximum(h1 @ W2.T + b2, 0)
+    return h2 @ W3.T + b3
+
+
+def head_accuracy(X, Y, w):
+    z = forward_np(np.asarray(X, np.float64), w)
+    acc = {}
+    for name, (lo, n), col in (("side", (0, 2), 0), ("direction", (2, 2), 1), ("variant", (4, 3), 2)):
+        m = Y[:, col] >= 0
+        pred = np.argmax(z[m, lo:lo + n], axis=1)
+        acc[name] = float((pred == Y[m, col]).mean()) if m.any() else None
+    return acc
+
+
+if __name__ == "__main__":
+    main()

@@ -67,7 +67,7 @@ typedef struct fc_opts {
     void   *stream;       /* cudaStream_t, NULL = the library's own stream  */
     int32_t cta_work_k;   /* work-sharing engine: a step reading more than
                              cta_work_k * 1024 adjacency entries is cut into
-                             tiles that every CTA may take (0 = 16 for
+                             tiles that every CTA may take (0 = 8 for
                              batches, 4 for single queries; < 0 = share
                              every step)                                    */
     int32_t variant;      /* top-down expansion variant: 0 = chosen by the
@@ -183,6 +183,41 @@ int fc_stcon_batch_device(fc_graph *const *gs, int32_t ngraphs, const int32_t *d
                           const int32_t *d_s, const int32_t *d_t, int32_t nq,
                           int32_t *d_connected, int32_t *d_hops, const fc_opts *opts,
                           fc_stats *stats);
+
+/* ---- learned schedule (no counterpart in the reference) ------------------ */
+
+/* Install the MLP weights of FC_SCHED_LEARNED for the current device: 1,703
+ * floats, W1[32][12] b1[32] W2[32][32] b2[32] W3[7][32] b3[7]; logits 0-1
+ * pick the side, 2-3 top-down / bottom-up, 4-6 the expansion variant.  The
+ * network reads 12 features per step (frontier sizes and adjacency sums of
+ * both sides, unexplored fraction, last side, frontier degree histograms). */
+int fc_sched_set_weights(const float *w, int32_t n);
+int fc_sched_get_weights(float *w, int32_t n);
+
+/* Training kernels.  X: n x 12 features, Y: n x 3 labels (side, direction,
+ * variant; -1 = no label).  fc_mlp_loss_grad: mean softmax cross-entropy and
+ * its gradient at weights w (for gradient checks).  fc_mlp_train: `epochs`
+ * passes of mini-batch Adam over the samples in the given order; w_inout
+ * holds the initial weights and receives the trained ones; loss_curve
+ * (nullable, `epochs` floats) gets each epoch's mean loss. */
+int fc_mlp_loss_grad(const float *X, const int32_t *Y, int32_t n, const float *w, float *grad,
+                     float *loss);
+int fc_mlp_train(const float *X, const int32_t *Y, int32_t n, int32_t epochs, int32_t batch,
+                 float lr, float *w_inout, float *loss_curve);
+
+/* Batched s-t queries with training-data hooks (device arrays, synchronous).
+ * d_script (nullable): script_len action bytes per query forcing its first
+ * steps (bit 0 side, bit 1 bottom-up, bits 2-3 variant + 1; 0xFF = let the
+ * schedule decide); after the script the schedule of `opts` continues.
+ * d_trace (nullable): one record of 24 ints per executed step (query, step,
+ * side, direction, variant, met, entries read lo/hi, ns lo/hi, vertices
+ * claimed, frontier size, 12 float features as bit patterns), at most
+ * trace_cap records, *d_trace_count = records produced.  d_inspected
+ * (nullable): adjacency entries read per query. */
+int fc_stcon_batch_scripted(fc_graph *g, const int32_t *d_s, const int32_t *d_t, int32_t nq,
+                            const uint8_t *d_script, int32_t script_len, const fc_opts *opts,
+                            int32_t *d_hops, int64_t *d_inspected, int32_t *d_trace,
+                            int32_t trace_cap, int32_t *d_trace_count);
 
 /* Batch of s-t queries that allocates nothing (no counterpart in the
  * reference).  For callers that cannot allocate device memory while they
