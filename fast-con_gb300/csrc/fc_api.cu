@@ -457,6 +457,12 @@ int fc_graph_from_csr(const int32_t *row_ptr, int32_t nv, const int32_t *col, in
         set_error("copy of the CSR failed");
         return FC_ERR_CUDA;
     }
+    // the copies above ran on the legacy stream; later kernels use others
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        fc_graph_free(gg);
+        set_error("copy of the CSR failed");
+        return FC_ERR_CUDA;
+    }
     rc = finish_graph(gg, st);
     if (rc) {
         fc_graph_free(gg);

@@ -233,6 +233,9 @@ DevCtx *get_ctx(int *err)
             return nullptr;
         }
         cudaMemset(c->tc, 0, sizeof(TeamCounters));
+        // set-up work runs on the legacy stream; the traversal kernels run on
+        // non-blocking streams, which do not wait for it: finish it here
+        cudaDeviceSynchronize();
         c->device = dev;
     }
     *err = FC_OK;
@@ -254,6 +257,7 @@ static int ensure_ws(DevCtx *c, size_t nv)
     FC_CUDA_TRY(cudaMalloc(&c->levels, nv * sizeof(int32_t)));
     FC_CUDA_TRY(cudaMalloc(&c->log, nv * sizeof(int32_t)));
     FC_CUDA_TRY(cudaMemset(c->status, 0xFF, sbytes));
+    FC_CUDA_TRY(cudaDeviceSynchronize());  // before any kernel on another stream reads it
     c->ws_nv = nv;
     return FC_OK;
 }
@@ -313,6 +317,7 @@ static int check_counters(DevCtx *c, cudaStream_t st)
         // leave the workspace clean for the next call
         cudaMemset(c->tc, 0, sizeof(TeamCounters));
         if (c->status) cudaMemset(c->status, 0xFF, (c->ws_nv + 15) / 16 * 16);
+        cudaDeviceSynchronize();
         return FC_ERR_TIMEOUT;
     }
     return FC_OK;
@@ -433,6 +438,7 @@ static int ensure_pool(DevCtx *c)
     FC_CUDA_TRY(cudaMalloc(&c->p_jobs, pool_job_bytes() * (size_t)grid));
     FC_CUDA_TRY(cudaMemset(c->p_slots, 0, pool_slot_bytes() * (size_t)grid));
     FC_CUDA_TRY(cudaMemset(c->p_jobs, 0, pool_job_bytes() * (size_t)grid));
+    FC_CUDA_TRY(cudaDeviceSynchronize());
     c->p_grid = grid;
     return FC_OK;
 }
@@ -449,6 +455,7 @@ static int check_pool(DevCtx *c, cudaStream_t st, int *invalid)
         cudaMemset(c->p_slots, 0, pool_slot_bytes() * (size_t)c->p_grid);
         if (c->status) cudaMemset(c->status, 0xFF, (c->ws_nv + 15) / 16 * 16);
         if (c->b_status) cudaMemset(c->b_status, 0xFF, c->b_slots * c->b_status_stride);
+        cudaDeviceSynchronize();
         return FC_ERR_TIMEOUT;
     }
     return FC_OK;
@@ -648,6 +655,7 @@ static int ensure_batch_arena(DevCtx *c, size_t slots, size_t maxnv, int log_cap
     FC_CUDA_TRY(cudaMalloc(&c->b_status, slots * sstride));
     FC_CUDA_TRY(cudaMalloc(&c->b_log, slots * lstride * sizeof(int32_t)));
     FC_CUDA_TRY(cudaMemset(c->b_status, 0xFF, slots * sstride));
+    FC_CUDA_TRY(cudaDeviceSynchronize());  // the pool kernel runs on another stream
     c->b_slots = slots;
     c->b_status_stride = sstride;
     c->b_log_stride = lstride;

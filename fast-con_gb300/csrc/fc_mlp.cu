@@ -4,7 +4,9 @@
 // Network (fc_sched.cuh): 12 features -> 32 ReLU -> 32 ReLU -> 7 logits in
 // three heads: side (logits 0-1), direction (2-3), expansion variant (4-6).
 // Loss: softmax cross-entropy per head, summed over the heads that carry a
-// label (label -1 = none), averaged over the samples of the batch.
+// label (label -1 = none), each head's term multiplied by the sample's weight
+// for that head (1 when no weights are given; training uses the cost of a
+// wrong choice), averaged over the samples of the batch.
 //
 // Kernels:
 //   k_mlp_grad   one warp per sample: lane j owns hidden unit j in the
@@ -26,7 +28,8 @@ namespace fc {
 constexpr int MLP_BLOCK = 256;
 
 __global__ void __launch_bounds__(MLP_BLOCK) k_mlp_grad(const float *__restrict__ X,
-                                                        const int32_t *__restrict__ Y, int n,
+                                                        const int32_t *__restrict__ Y,
+                                                        const float *__restrict__ SW, int n,
                                                         const float *__restrict__ W,
                                                         float *__restrict__ grad, float *loss_sum,
                                                         float scale)
@@ -60,6 +63,7 @@ __global__ void __launch_bounds__(MLP_BLOCK) k_mlp_grad(const float *__restrict_
         float L = 0.f;
         for (int h = 0; h < 3; ++h) {
             const int label = y[h];
+            const float wgt = SW ? SW[(size_t)smp * 3 + h] : 1.f;
             float mx = z[lo[h]];
             for (int k = 1; k < len[h]; ++k) mx = fmaxf(mx, z[lo[h] + k]);
             float se = 0.f;
@@ -69,10 +73,10 @@ __global__ void __launch_bounds__(MLP_BLOCK) k_mlp_grad(const float *__restrict_
                     dz[lo[h] + k] = 0.f;
                 } else {
                     const float p = expf(z[lo[h] + k] - mx) / se;
-                    dz[lo[h] + k] = (p - (k == label ? 1.f : 0.f)) * scale;
+                    dz[lo[h] + k] = (p - (k == label ? 1.f : 0.f)) * scale * wgt;
                 }
             }
-            if (label >= 0) L += logf(se) + mx - z[lo[h] + label];
+            if (label >= 0) L += wgt * (logf(se) + mx - z[lo[h] + label]);
         }
         loss_acc += L;
         // backward
@@ -128,6 +132,7 @@ int set_mlp_weights(DevCtx *c, const float *w)
 {
     if (!c->d_mlp) FC_CUDA_TRY(cudaMalloc(&c->d_mlp, sizeof(float) * MLP_PARAMS));
     FC_CUDA_TRY(cudaMemcpy(c->d_mlp, w, sizeof(float) * MLP_PARAMS, cudaMemcpyHostToDevice));
+    FC_CUDA_TRY(cudaDeviceSynchronize());  // read by kernels on non-blocking streams
     std::memcpy(c->h_mlp, w, sizeof(float) * MLP_PARAMS);
     c->mlp_ready = 1;
     return FC_OK;
@@ -166,15 +171,19 @@ extern "C" int fc_sched_get_weights(float *w, int32_t n)
 }
 
 // One forward/backward pass over (X, Y); grad receives the mean gradient.
-extern "C" int fc_mlp_loss_grad(const float *X, const int32_t *Y, int32_t n, const float *w,
-                                float *grad, float *loss)
+extern "C" int fc_mlp_loss_grad(const float *X, const int32_t *Y, const float *SW, int32_t n,
+                                const float *w, float *grad, float *loss)
 {
     if (!X || !Y || !w || !grad || !loss || n <= 0) return FC_ERR_INVALID;
     int rc = FC_OK;
     DevCtx *c = get_ctx(&rc);
     if (!c) return rc;
-    float *dX = nullptr, *dW = nullptr, *dG = nullptr, *dL = nullptr;
+    float *dX = nullptr, *dW = nullptr, *dG = nullptr, *dL = nullptr, *dS = nullptr;
     int32_t *dY = nullptr;
+    if (SW) {
+        FC_CUDA_TRY(cudaMalloc(&dS, sizeof(float) * (size_t)n * 3));
+        FC_CUDA_TRY(cudaMemcpy(dS, SW, sizeof(float) * (size_t)n * 3, cudaMemcpyHostToDevice));
+    }
     FC_CUDA_TRY(cudaMalloc(&dX, sizeof(float) * (size_t)n * MLP_IN));
     FC_CUDA_TRY(cudaMalloc(&dY, sizeof(int32_t) * (size_t)n * 3));
     FC_CUDA_TRY(cudaMalloc(&dW, sizeof(float) * MLP_PARAMS));
@@ -184,7 +193,7 @@ extern "C" int fc_mlp_loss_grad(const float *X, const int32_t *Y, int32_t n, con
     FC_CUDA_TRY(cudaMemcpy(dY, Y, sizeof(int32_t) * (size_t)n * 3, cudaMemcpyHostToDevice));
     FC_CUDA_TRY(cudaMemcpy(dW, w, sizeof(float) * MLP_PARAMS, cudaMemcpyHostToDevice));
     FC_CUDA_TRY(cudaMemset(dG, 0, sizeof(float) * (MLP_PARAMS + 1)));
-    k_mlp_grad<<<mlp_grid(n), MLP_BLOCK>>>(dX, dY, n, dW, dG, dL, 1.f / (float)n);
+    k_mlp_grad<<<mlp_grid(n), MLP_BLOCK>>>(dX, dY, dS, n, dW, dG, dL, 1.f / (float)n);
     FC_CUDA_TRY(cudaGetLastError());
     FC_CUDA_TRY(cudaMemcpy(grad, dG, sizeof(float) * MLP_PARAMS, cudaMemcpyDeviceToHost));
     float ls = 0;
@@ -194,21 +203,27 @@ extern "C" int fc_mlp_loss_grad(const float *X, const int32_t *Y, int32_t n, con
     cudaFree(dY);
     cudaFree(dW);
     cudaFree(dG);
+    cudaFree(dS);
     return FC_OK;
 }
 
 // Mini-batch Adam training on the GPU.  w_inout holds the initial weights and
 // receives the trained ones; loss_curve (nullable) gets the mean training loss
 // of each epoch.  Samples are visited in a fixed order (the caller shuffles).
-extern "C" int fc_mlp_train(const float *X, const int32_t *Y, int32_t n, int32_t epochs,
-                            int32_t batch, float lr, float *w_inout, float *loss_curve)
+extern "C" int fc_mlp_train(const float *X, const int32_t *Y, const float *SW, int32_t n,
+                            int32_t epochs, int32_t batch, float lr, float *w_inout,
+                            float *loss_curve)
 {
     if (!X || !Y || !w_inout || n <= 0 || epochs <= 0 || batch <= 0) return FC_ERR_INVALID;
     int rc = FC_OK;
     DevCtx *c = get_ctx(&rc);
     if (!c) return rc;
-    float *dX = nullptr, *dW = nullptr, *dG = nullptr, *dM = nullptr, *dV = nullptr;
+    float *dX = nullptr, *dW = nullptr, *dG = nullptr, *dM = nullptr, *dV = nullptr, *dS = nullptr;
     int32_t *dY = nullptr;
+    if (SW) {
+        FC_CUDA_TRY(cudaMalloc(&dS, sizeof(float) * (size_t)n * 3));
+        FC_CUDA_TRY(cudaMemcpy(dS, SW, sizeof(float) * (size_t)n * 3, cudaMemcpyHostToDevice));
+    }
     FC_CUDA_TRY(cudaMalloc(&dX, sizeof(float) * (size_t)n * MLP_IN));
     FC_CUDA_TRY(cudaMalloc(&dY, sizeof(int32_t) * (size_t)n * 3));
     FC_CUDA_TRY(cudaMalloc(&dW, sizeof(float) * MLP_PARAMS * 4 + sizeof(float) * 4));
@@ -227,8 +242,9 @@ extern "C" int fc_mlp_train(const float *X, const int32_t *Y, int32_t n, int32_t
         for (int b0 = 0; b0 < n; b0 += batch) {
             const int nb = n - b0 < batch ? n - b0 : batch;
             FC_CUDA_TRY(cudaMemset(dG, 0, sizeof(float) * MLP_PARAMS));
-            k_mlp_grad<<<mlp_grid(nb), MLP_BLOCK>>>(dX + (size_t)b0 * MLP_IN, dY + (size_t)b0 * 3, nb,
-                                                    dW, dG, dL, 1.f / (float)nb);
+            k_mlp_grad<<<mlp_grid(nb), MLP_BLOCK>>>(dX + (size_t)b0 * MLP_IN, dY + (size_t)b0 * 3,
+                                                    dS ? dS + (size_t)b0 * 3 : nullptr, nb, dW, dG,
+                                                    dL, 1.f / (float)nb);
             p1 *= b1;
             p2 *= b2;
             k_adam<<<(MLP_PARAMS + 255) / 256, 256>>>(dW, dG, dM, dV, MLP_PARAMS, lr, b1, b2, eps,
@@ -245,5 +261,6 @@ extern "C" int fc_mlp_train(const float *X, const int32_t *Y, int32_t n, int32_t
     cudaFree(dX);
     cudaFree(dY);
     cudaFree(dW);
+    cudaFree(dS);
     return FC_OK;
 }

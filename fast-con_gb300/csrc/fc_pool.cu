@@ -435,7 +435,11 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
                 }
                 const int x = sm.ql.side;
                 const long long m = (long long)(sm.ql.dt[x] - sm.ql.dh[x]);
-                if (!a.exclusive && (long long)sm.ql.tail[0] + sm.ql.tail[1] + m > cap) {
+                // new claims are bounded by the entries read and by the
+                // vertices not yet claimed
+                const long long used = (long long)sm.ql.tail[0] + sm.ql.tail[1];
+                const long long grow = m < (long long)nv - used ? m : (long long)nv - used;
+                if (!a.exclusive && used + grow > cap) {
                     sm.ql.escalate = 1;  // the log could overflow: finish it in exclusive mode
                     sm.ql.done = 1;
                 }

@@ -266,13 +266,28 @@ __device__ __forceinline__ void mlp_forward_warp(const float *__restrict__ W, co
     }
 }
 
-// Turn logits (or a scripted action) into the step, within the engine's
-// constraints: one side only for BFS, bottom-up only where allowed.
+// Turn logits into the step, within the engine's constraints (one side only
+// for BFS, bottom-up only where allowed).  The side and direction heads
+// override the heuristic's choice (already in q) only when confident: a logit
+// margin above MLP_MARGIN (softmax probability above 0.75); otherwise the
+// fixed-threshold heuristic stands.  The variant head always decides.
+constexpr float MLP_MARGIN = 1.0986f;  // ln 3
+
 __host__ __device__ inline void ql_apply_logits(QLocal &q, const float *o, int allow_bu,
                                                 int bu_level_cap)
 {
-    q.side = q.two ? (o[1] > o[0] ? 1 : 0) : 0;
-    q.dir = (allow_bu && q.radius[q.side] + 1 <= bu_level_cap && o[3] > o[2]) ? DIR_BU : DIR_TD;
+    const int side0 = q.side;
+    if (q.two) {
+        const float d = o[1] - o[0];
+        if (d > MLP_MARGIN) q.side = 1;
+        else if (d < -MLP_MARGIN) q.side = 0;
+    }
+    const float db = o[3] - o[2];
+    const bool bu_ok = allow_bu && q.radius[q.side] + 1 <= bu_level_cap;
+    if (db > MLP_MARGIN && bu_ok)
+        q.dir = DIR_BU;
+    else if (db < -MLP_MARGIN || !bu_ok || q.side != side0)
+        q.dir = DIR_TD;
     int v = 0;
     if (o[5] > o[4 + v]) v = 1;
     if (o[6] > o[4 + v]) v = 2;

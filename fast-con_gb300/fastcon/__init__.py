@@ -109,8 +109,9 @@ def lib():
                                                       _I32, _VP, _VP, _I32, _VP]),
             "fc_sched_set_weights": (ctypes.c_int, [_VP, _I32]),
             "fc_sched_get_weights": (ctypes.c_int, [_VP, _I32]),
-            "fc_mlp_loss_grad": (ctypes.c_int, [_VP, _VP, _I32, _VP, _VP, _VP]),
-            "fc_mlp_train": (ctypes.c_int, [_VP, _VP, _I32, _I32, _I32, ctypes.c_float, _VP, _VP]),
+            "fc_mlp_loss_grad": (ctypes.c_int, [_VP, _VP, _VP, _I32, _VP, _VP, _VP]),
+            "fc_mlp_train": (ctypes.c_int, [_VP, _VP, _VP, _I32, _I32, _I32, ctypes.c_float, _VP,
+                                            _VP]),
             "fc_stcon_batch_scripted": (ctypes.c_int, [_VP, _VP, _VP, _I32, _VP, _I32, _VP, _VP,
                                                        _VP, _VP, _I32, _VP]),
             "fc_strerror": (ctypes.c_char_p, [ctypes.c_int]),

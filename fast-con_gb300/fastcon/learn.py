@@ -65,23 +65,32 @@ def load_default_weights(path: str = WEIGHTS_PATH) -> dict:
     return d
 
 
-def loss_grad(X: np.ndarray, Y: np.ndarray, w: np.ndarray):
+def _sw(SW, n):
+    if SW is None:
+        return None, None
+    SW = np.ascontiguousarray(SW, dtype=np.float32).reshape(n, 3)
+    return SW, SW.ctypes.data
+
+
+def loss_grad(X: np.ndarray, Y: np.ndarray, w: np.ndarray, SW=None):
     X = np.ascontiguousarray(X, dtype=np.float32)
     Y = np.ascontiguousarray(Y, dtype=np.int32)
     w = np.ascontiguousarray(w, dtype=np.float32)
+    SW, swp = _sw(SW, len(X))
     g = np.zeros(N_PARAMS, np.float32)
     loss = np.zeros(1, np.float32)
-    _check(lib().fc_mlp_loss_grad(X.ctypes.data, Y.ctypes.data, len(X), w.ctypes.data,
+    _check(lib().fc_mlp_loss_grad(X.ctypes.data, Y.ctypes.data, swp, len(X), w.ctypes.data,
                                   g.ctypes.data, loss.ctypes.data), "fc_mlp_loss_grad")
     return float(loss[0]), g
 
 
-def train(X, Y, epochs=40, batch=256, lr=3e-3, seed=0, w0=None):
+def train(X, Y, epochs=40, batch=256, lr=3e-3, seed=0, w0=None, SW=None):
     X = np.ascontiguousarray(X, dtype=np.float32)
     Y = np.ascontiguousarray(Y, dtype=np.int32)
+    SW, swp = _sw(SW, len(X))
     w = init_weights(seed) if w0 is None else np.array(w0, dtype=np.float32)
     curve = np.zeros(epochs, np.float32)
-    _check(lib().fc_mlp_train(X.ctypes.data, Y.ctypes.data, len(X), epochs, batch,
+    _check(lib().fc_mlp_train(X.ctypes.data, Y.ctypes.data, swp, len(X), epochs, batch,
                               ctypes.c_float(lr), w.ctypes.data, curve.ctypes.data),
            "fc_mlp_train")
     return w, curve
@@ -122,8 +131,14 @@ def run_scripted(G: Graph, s, t, script=None, sched=SCHED_HEURISTIC, variant=0, 
 
 
 def decode(recs: np.ndarray):
-    """Trace records -> dict of arrays."""
+    """Trace records -> dict of arrays.  A query that outgrew its slot is run
+    again from the start in the exclusive pass; its later records replace the
+    earlier ones (the last record of each (query, step) is kept)."""
     r = recs
+    if len(r):
+        key = r[:, 0].astype(np.int64) * (1 << 20) + r[:, 1]
+        _, last = np.unique(key[::-1], return_index=True)
+        r = r[np.sort(len(r) - 1 - last)]
     return {
         "q": r[:, 0], "step": r[:, 1], "side": r[:, 2], "dir": r[:, 3], "variant": r[:, 4],
         "met": r[:, 5],
@@ -156,7 +171,7 @@ def label_states(G: Graph, s, t, tr, max_states: int, rng):
         pick = rng.choice(len(states), size=max_states, replace=False)
         states = [states[i] for i in sorted(pick)]
     if not states:
-        return np.zeros((0, 12), np.float32), np.zeros((0, 3), np.int32), []
+        return np.zeros((0, 12), np.float32), np.zeros((0, 3), np.int32), np.zeros((0, 3), np.float32), []
     L = max(k for _, k in states) + 1
     rs, rt, scripts = [], [], []
     for q, k in states:
@@ -170,13 +185,24 @@ def label_states(G: Graph, s, t, tr, max_states: int, rng):
             rt.append(t[q])
     hops, ins, _ = run_scripted(G, np.array(rs), np.array(rt), np.stack(scripts),
                                 sched=SCHED_HEURISTIC)
-    ins = ins.reshape(len(states), len(CANDIDATES))
-    best = np.argmin(ins, axis=1)  # argmin keeps the first minimum
+    C = ins.reshape(len(states), len(CANDIDATES)).astype(np.float64)
+    best = np.argmin(C, axis=1)  # argmin keeps the first minimum
     X = np.stack([tr["feat"][acts[q][k][3]] for q, k in states]).astype(np.float32)
     Y = np.full((len(states), 3), -1, np.int32)
-    Y[:, 0] = [CANDIDATES[b][0] for b in best]
-    Y[:, 1] = [CANDIDATES[b][1] for b in best]
-    return X, Y, [(q, k) for q, k in states]
+    SW = np.ones((len(states), 3), np.float32)
+    bs = np.array([CANDIDATES[b][0] for b in best])
+    bd = np.array([CANDIDATES[b][1] for b in best])
+    Y[:, 0] = bs
+    Y[:, 1] = bd
+    cbest = C[np.arange(len(states)), best]
+    # cost of the wrong side (its best direction) and of the wrong direction
+    other_side = np.where(bs == 0, np.minimum(C[:, 1], C[:, 3]), np.minimum(C[:, 0], C[:, 2]))
+    other_dir = np.where(bd == 0, np.where(bs == 0, C[:, 2], C[:, 3]),
+                         np.where(bs == 0, C[:, 0], C[:, 1]))
+    denom = np.maximum(cbest, 1.0)
+    SW[:, 0] = np.clip(np.log2(1.0 + (other_side - cbest) / denom), 0.02, 8.0)
+    SW[:, 1] = np.clip(np.log2(1.0 + (other_dir - cbest) / denom), 0.02, 8.0)
+    return X, Y, SW, [(q, k) for q, k in states]
 
 
 def label_variants(G: Graph, s, t, tr, states):
@@ -197,18 +223,19 @@ def label_variants(G: Graph, s, t, tr, states):
         for i in range(len(d["q"])):
             tm[(int(d["q"][i]), int(d["step"][i]))] = int(d["ns"][i])
         times.append(tm)
-    lab = []
+    lab, wv = [], []
     for q, k in states:
-        ts = [tm.get((q, k), 1 << 62) for tm in times]
-        lab.append(int(np.argmin(ts)))
-    return np.array(lab, np.int32)
+        ts = np.array([tm.get((q, k), 1 << 62) for tm in times], np.float64)
+        b = int(np.argmin(ts))
+        lab.append(b)
+        rest = np.delete(ts, b)
+        wv.append(np.clip(np.log2(1.0 + (rest.min() - ts[b]) / max(ts[b], 1.0)), 0.02, 4.0))
+    return np.array(lab, np.int32), np.array(wv, np.float32)
 
 
-def build_dataset(total_queries=20000, scales=(18, 19, 20, 21, 22), first_seed=1000,
-                  states_per_graph=6000, seed=0, log=print):
-    rng = np.random.default_rng(seed)
+def training_graphs(total_queries=20000, scales=(18, 19, 20, 21, 22), first_seed=1000):
+    """(graph, s, t) of the training set: two R-MAT graphs per scale."""
     per_graph = total_queries // (2 * len(scales))
-    Xs, Ys = [], []
     gi = 0
     for rep in range(2):
         for sc in scales:
@@ -217,21 +244,41 @@ def build_dataset(total_queries=20000, scales=(18, 19, 20, 21, 22), first_seed=1
             G = Graph.rmat(sc, 8 << sc, seed=gseed, perm_seed=gseed)
             rp, _ = G.csr_row_ptr()
             s, t = graphs.pairs_with_degree(np.diff(rp), per_graph, seed=gseed + 500)
-            for pol in (SCHED_PLAIN, SCHED_HEURISTIC):
-                _, _, rec = run_scripted(G, s, t, None, sched=pol, trace=True)
-                tr = decode(rec)
-                X, Y, states = label_states(G, s, t, tr, states_per_graph // 2, rng)
-                Y[:, 2] = label_variants(G, s, t, tr, states)
-                Xs.append(X)
-                Ys.append(Y)
-                log(f"graph scale {sc} seed {gseed} policy {pol}: {len(X)} states, "
-                    f"labels side1 {Y[:, 0].mean():.2f} bu {Y[:, 1].mean():.2f} "
-                    f"variant {np.bincount(Y[:, 2], minlength=3).tolist()}")
-            G.free()
-    X = np.concatenate(Xs)
-    Y = np.concatenate(Ys)
+            yield sc, gseed, G, s, t
+
+
+def label_policy_states(G, s, t, pol, nstates, rng, log=print, tag=""):
+    t0 = time.time()
+    _, _, rec = run_scripted(G, s, t, None, sched=pol, trace=True)
+    tr = decode(rec)
+    t1 = time.time()
+    X, Y, SW, states = label_states(G, s, t, tr, nstates, rng)
+    t2 = time.time()
+    Y[:, 2], SW[:, 2] = label_variants(G, s, t, tr, states)
+    t3 = time.time()
+    log(f"{tag} policy {pol}: {len(X)} states, side1 {Y[:, 0].mean():.2f} "
+        f"bu {Y[:, 1].mean():.3f} variant {np.bincount(Y[:, 2], minlength=3).tolist()} "
+        f"(trace {t1 - t0:.1f}s, rollouts {t2 - t1:.1f}s, variants {t3 - t2:.1f}s)")
+    return X, Y, SW
+
+
+def build_dataset(total_queries=20000, states_per_graph=6000, seed=0, policies=None, log=print):
+    """States from the plain and heuristic traces (and from the learned
+    schedule when weights are loaded and SCHED_LEARNED is listed)."""
+    rng = np.random.default_rng(seed)
+    policies = policies or (SCHED_PLAIN, SCHED_HEURISTIC)
+    Xs, Ys, Ws = [], [], []
+    for sc, gseed, G, s, t in training_graphs(total_queries):
+        for pol in policies:
+            X, Y, SW = label_policy_states(G, s, t, pol, states_per_graph // len(policies), rng,
+                                           log, f"scale {sc} seed {gseed}")
+            Xs.append(X)
+            Ys.append(Y)
+            Ws.append(SW)
+        G.free()
+    X, Y, SW = np.concatenate(Xs), np.concatenate(Ys), np.concatenate(Ws)
     perm = rng.permutation(len(X))
-    return X[perm], Y[perm]
+    return X[perm], Y[perm], SW[perm]
 
 
 # ---------------------------------------------------------------------------
@@ -264,13 +311,24 @@ def main():
     ap.add_argument("--eval-queries", type=int, default=4096)
     args = ap.parse_args()
     t0 = time.time()
-    X, Y = build_dataset(args.queries)
+    X, Y, SW = build_dataset(args.queries)
     t1 = time.time()
     nval = len(X) // 10
-    w, curve = train(X[nval:], Y[nval:], epochs=args.epochs)
-    vloss, _ = loss_grad(X[:nval], Y[:nval], w)
+    w, curve = train(X[nval:], Y[nval:], epochs=args.epochs, SW=SW[nval:])
+    # second round: label the states the learned schedule itself visits
+    set_weights(w)
+    X2, Y2, SW2 = build_dataset(args.queries, states_per_graph=3000, seed=1,
+                                policies=(SCHED_LEARNED,))
+    X = np.concatenate([X, X2])
+    Y = np.concatenate([Y, Y2])
+    SW = np.concatenate([SW, SW2])
+    perm = np.random.default_rng(2).permutation(len(X))
+    X, Y, SW = X[perm], Y[perm], SW[perm]
+    w, curve = train(X[nval:], Y[nval:], epochs=args.epochs, SW=SW[nval:], w0=w)
+    vloss, _ = loss_grad(X[:nval], Y[:nval], w, SW[:nval])
     # validation accuracy per head (host forward pass in float64)
     acc = head_accuracy(X[:nval], Y[:nval], w)
+    acc_heur = heuristic_accuracy(X[:nval], Y[:nval])
     t2 = time.time()
     set_weights(w)
     ev = {}
@@ -294,6 +352,8 @@ def main():
                      "samples": int(len(X) - nval), "validation": int(nval),
                      "epochs": args.epochs, "loss_curve": [float(x) for x in curve],
                      "validation_loss": vloss, "validation_accuracy": acc,
+                     "heuristic_side_accuracy": acc_heur,
+                     "rounds": "plain + heuristic traces, then the learned schedule's own states",
                      "label_balance": {"side1": float(Y[:, 0].mean()), "bottom_up": float(Y[:, 1].mean()),
                                        "variant": np.bincount(Y[:, 2], minlength=3).tolist()},
                      "seconds": {"dataset": t1 - t0, "train": t2 - t1}},
@@ -316,6 +376,14 @@ def forward_np(X, w):
     h1 = np.maximum(X @ W1.T + b1, 0)
     h2 = np.maximum(h1 @ W2.T + b2, 0)
     return h2 @ W3.T + b3
+
+
+def heuristic_accuracy(X, Y):
+    """How often the fixed rule (smaller frontier edge sum first) agrees with
+    the side label (features 2 and 3 are log2 of the edge sums)."""
+    pred = (X[:, 3] < X[:, 2]).astype(np.int32)
+    m = Y[:, 0] >= 0
+    return float((pred[m] == Y[m, 0]).mean()) if m.any() else None
 
 
 def head_accuracy(X, Y, w):

@@ -195,15 +195,16 @@ int fc_sched_set_weights(const float *w, int32_t n);
 int fc_sched_get_weights(float *w, int32_t n);
 
 /* Training kernels.  X: n x 12 features, Y: n x 3 labels (side, direction,
- * variant; -1 = no label).  fc_mlp_loss_grad: mean softmax cross-entropy and
- * its gradient at weights w (for gradient checks).  fc_mlp_train: `epochs`
- * passes of mini-batch Adam over the samples in the given order; w_inout
- * holds the initial weights and receives the trained ones; loss_curve
- * (nullable, `epochs` floats) gets each epoch's mean loss. */
-int fc_mlp_loss_grad(const float *X, const int32_t *Y, int32_t n, const float *w, float *grad,
-                     float *loss);
-int fc_mlp_train(const float *X, const int32_t *Y, int32_t n, int32_t epochs, int32_t batch,
-                 float lr, float *w_inout, float *loss_curve);
+ * variant; -1 = no label), SW (nullable): n x 3 per-head sample weights.
+ * fc_mlp_loss_grad: mean weighted softmax cross-entropy and its gradient at
+ * weights w (for gradient checks).  fc_mlp_train: `epochs` passes of
+ * mini-batch Adam over the samples in the given order; w_inout holds the
+ * initial weights and receives the trained ones; loss_curve (nullable,
+ * `epochs` floats) gets each epoch's mean loss. */
+int fc_mlp_loss_grad(const float *X, const int32_t *Y, const float *SW, int32_t n, const float *w,
+                     float *grad, float *loss);
+int fc_mlp_train(const float *X, const int32_t *Y, const float *SW, int32_t n, int32_t epochs,
+                 int32_t batch, float lr, float *w_inout, float *loss_curve);
 
 /* Batched s-t queries with training-data hooks (device arrays, synchronous).
  * d_script (nullable): script_len action bytes per query forcing its first

@@ -394,3 +394,22 @@ def test_shared_steps_and_row_jobs(fastcon_lib, oracle_mod):
             for src in (0, 1, 50000, 7):
                 lev, _ = oracle_mod.bfs_levels(rp, col, src)
                 assert (G.bfs_levels(src, o) == lev).all(), (work_k, sch, src)
+
+
+# --------------------------------------------------------------------------
+# the first batch on a graph bigger than any before it: the workspaces are
+# reallocated and initialised, and must be ready before the kernels run
+# --------------------------------------------------------------------------
+def test_first_call_after_workspace_growth(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    scale = 20
+    u, v = graphs.rmat_edges(scale, 8 << scale, seed=81, perm_seed=82)
+    G = fc.Graph.from_edges(u, v, 1 << scale)
+    rp, col = G.csr()
+    s, t = graphs.pairs_with_degree(np.diff(rp), 2000, seed=83)
+    conn, hops = fc.stcon_batch(G, s, t, opts=opts(fc, "batched", "plain"))
+    samp = np.arange(0, 2000, 7)
+    _, want, _ = oracle_mod.stcon_batch(rp, col, s[samp], t[samp], nthreads=16)
+    assert (hops[samp] == want).all()
+    conn2, hops2 = fc.stcon_batch(G, s, t, opts=opts(fc, "batched", "heuristic"))
+    assert (hops2 == hops).all()

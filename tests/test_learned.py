@@ -18,8 +18,9 @@ def unpack(w):
             w[1472:1696].reshape(7, 32), w[1696:1703])
 
 
-def loss_grad_np(X, Y, w):
-    """Mean softmax cross-entropy over labelled heads and its gradient, float64."""
+def loss_grad_np(X, Y, w, SW=None):
+    """Mean (weighted) softmax cross-entropy over labelled heads and its
+    gradient, float64."""
     W1, b1, W2, b2, W3, b3 = unpack(w)
     X = np.asarray(X, np.float64)
     n = len(X)
@@ -37,11 +38,12 @@ def loss_grad_np(X, Y, w):
         p = e / e.sum(axis=1, keepdims=True)
         lab = Y[:, col]
         m = lab >= 0
-        loss += (np.log(e.sum(axis=1))[m] + mx[m, 0] - zz[m, lab[m]]).sum()
+        wgt = np.ones(n) if SW is None else np.asarray(SW, np.float64)[:, col]
+        loss += (wgt[m] * (np.log(e.sum(axis=1))[m] + mx[m, 0] - zz[m, lab[m]])).sum()
         g = p.copy()
         g[m, lab[m]] -= 1.0
         g[~m] = 0.0
-        dz[:, lo:lo + k] = g
+        dz[:, lo:lo + k] = g * wgt[:, None]
     dz /= n
     gW3 = dz.T @ h2
     gb3 = dz.sum(0)
@@ -79,11 +81,12 @@ def test_restatement_matches_finite_differences():
 
 def test_gpu_gradient_matches_float64(fastcon_lib):
     from fastcon import learn
-    for seed in (5, 6):
+    for seed in (5, 6, 7):
         X, Y = random_set(300, seed)
         w = learn.init_weights(seed)
-        loss, g = learn.loss_grad(X, Y, w)
-        loss_ref, g_ref = loss_grad_np(X, Y, w)
+        SW = None if seed == 5 else np.random.default_rng(seed).uniform(0.02, 4, (300, 3))
+        loss, g = learn.loss_grad(X, Y, w, SW)
+        loss_ref, g_ref = loss_grad_np(X, Y, w, SW)
         assert abs(loss - loss_ref) <= 1e-4 * max(1.0, abs(loss_ref))
         # float32 accumulation vs float64: compare relative to the gradient norm
         err = np.abs(g - g_ref).max() / max(np.abs(g_ref).max(), 1e-12)
