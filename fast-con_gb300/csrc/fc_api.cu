@@ -708,6 +708,17 @@ int fc_stcon_batch_scripted(fc_graph *g, const int32_t *d_s, const int32_t *d_t,
     return rc;
 }
 
+int fc_selftest_wait(int32_t timeout_ms, double *elapsed_ms)
+{
+    if (timeout_ms < 1 || timeout_ms > 2000) {
+        set_error("timeout_ms %d outside [1, 2000]", timeout_ms);
+        return FC_ERR_INVALID;
+    }
+    CtxLock L;
+    if (!L.c) return L.rc;
+    return fc::engine_selftest_wait(L.c, timeout_ms, elapsed_ms, L.c->stream);
+}
+
 int fc_stcon_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *graph_idx, const int32_t *s,
                    const int32_t *t, int32_t nq, int32_t *connected, int32_t *hops,
                    const fc_opts *opts, fc_stats *stats)
@@ -734,9 +745,10 @@ int fc_stcon_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *graph_id
     CtxLock L;
     if (!L.c) return L.rc;
     cudaStream_t st = pick_stream(opts, L.c);
-    int32_t *buf = nullptr;
+    int rc = FC_OK;
     size_t k = (size_t)nq;
-    FC_CUDA_TRY(cudaMallocAsync(&buf, sizeof(int32_t) * k * 5, st));
+    int32_t *buf = fc::batch_staging(L.c, k, &rc);
+    if (!buf) return rc;
     int32_t *ds = buf, *dt = buf + k, *dg = buf + 2 * k, *dc = buf + 3 * k, *dh = buf + 4 * k;
     FC_CUDA_TRY(cudaMemcpyAsync(ds, s, sizeof(int32_t) * k, cudaMemcpyHostToDevice, st));
     FC_CUDA_TRY(cudaMemcpyAsync(dt, t, sizeof(int32_t) * k, cudaMemcpyHostToDevice, st));
@@ -744,14 +756,13 @@ int fc_stcon_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *graph_id
     std::vector<fc::GraphPairH> pairs((size_t)ngraphs);
     for (int i = 0; i < ngraphs; ++i) pairs[(size_t)i] = pair_of(gs[i]);
     fc_opts o = opts ? *opts : default_opts();
-    int rc = fc::engine_stcon_batch(L.c, pairs.data(), ngraphs, graph_idx ? dg : nullptr, ds, dt, nq,
-                                    dc, dh, o, stats, st, true);
+    rc = fc::engine_stcon_batch(L.c, pairs.data(), ngraphs, graph_idx ? dg : nullptr, ds, dt, nq,
+                                dc, dh, o, stats, st, true);
     if (rc == FC_OK) {
         FC_CUDA_TRY(cudaMemcpyAsync(connected, dc, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, st));
         FC_CUDA_TRY(cudaMemcpyAsync(hops, dh, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, st));
-        FC_CUDA_TRY(cudaStreamSynchronize(st));
     }
-    cudaFreeAsync(buf, st);
+    // the staging buffer is reused by the next call
     cudaStreamSynchronize(st);
     return rc;
 }

@@ -417,6 +417,53 @@ static int ensure_qstat(DevCtx *c, size_t n)
     return FC_OK;
 }
 
+int32_t *batch_staging(DevCtx *c, size_t n, int *rc)
+{
+    *rc = FC_OK;
+    if (c->b_stage && c->b_stage_cap >= n) return c->b_stage;
+    cudaFree(c->b_stage);
+    c->b_stage = nullptr;
+    c->b_stage_cap = 0;
+    size_t cap = n < 4096 ? 4096 : n;
+    cudaError_t e = cudaMalloc(&c->b_stage, sizeof(int32_t) * 5 * cap);
+    if (e != cudaSuccess) {
+        fc_set_last_cuda_error(e, "cudaMalloc(batch staging)", __FILE__, __LINE__);
+        *rc = e == cudaErrorMemoryAllocation ? FC_ERR_OOM : FC_ERR_CUDA;
+        return nullptr;
+    }
+    c->b_stage_cap = cap;
+    return c->b_stage;
+}
+
+// One CTA in a barrier sized for two: the wait can only expire.
+__global__ void k_wait_selftest(int *bar, int *err, unsigned long long timeout_ns)
+{
+    grid_barrier(bar, err, 2, timeout_ns);
+}
+
+int engine_selftest_wait(DevCtx *c, int timeout_ms, double *elapsed_ms, cudaStream_t stream)
+{
+    if (!c->selftest) FC_CUDA_TRY(cudaMalloc(&c->selftest, 4 * sizeof(int)));
+    FC_CUDA_TRY(cudaMemsetAsync(c->selftest, 0, 4 * sizeof(int), stream));
+    FC_CUDA_TRY(cudaEventRecord(c->ev0, stream));
+    k_wait_selftest<<<1, 32, 0, stream>>>(c->selftest, c->selftest + 2,
+                                          (unsigned long long)timeout_ms * 1000000ull);
+    FC_CUDA_TRY(cudaGetLastError());
+    FC_CUDA_TRY(cudaEventRecord(c->ev1, stream));
+    int h[4];
+    FC_CUDA_TRY(cudaMemcpyAsync(h, c->selftest, sizeof(h), cudaMemcpyDeviceToHost, stream));
+    FC_CUDA_TRY(cudaStreamSynchronize(stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    if (elapsed_ms) *elapsed_ms = ms;
+    if (h[2] == FC_ERR_TIMEOUT) {
+        set_error("device-side wait expired after %.1f ms (self-test)", ms);
+        return FC_ERR_TIMEOUT;
+    }
+    set_error("self-test: the wait did not report a timeout (flag %d)", h[2]);
+    return FC_ERR_CUDA;
+}
+
 static int ensure_tmp(DevCtx *c)
 {
     if (c->d_tmp_q) return FC_OK;
@@ -691,9 +738,12 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
     }
     const int engine = pick_engine(o, FC_ENGINE_BATCHED);
     int launches = 0;
+    int graph_use = 0;
     FC_CUDA_TRY(cudaEventRecord(c->ev0, stream));
-    FC_CUDA_TRY(cudaMemsetAsync(c->qstat, 0, sizeof(QueryStat) * (size_t)nq, stream));
-    FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 8 * sizeof(int), stream));
+    if (engine != FC_ENGINE_BATCHED) {
+        FC_CUDA_TRY(cudaMemsetAsync(c->qstat, 0, sizeof(QueryStat) * (size_t)nq, stream));
+        FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 8 * sizeof(int), stream));
+    }
     if (engine == FC_ENGINE_BATCHED) {
         if ((rc = ensure_pool(c))) return rc;
         // two owner CTAs per SM: with tile sharing more owners do not help and
@@ -745,9 +795,6 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.qstat = c->qstat;
         a.mlp = learned_weights(c, o);
         apply_extras(a, ex);
-        rc = pool_launch(a, grid, stream);
-        if (rc) return rc;
-        FC_CUDA_TRY(cudaEventRecord(c->evm, stream));
         // queries whose visit log outgrew their slot: one at a time, whole grid
         PoolArgs x = pool_args_exclusive(c, MODE_STCON, o);
         x.graph_idx = d_gi;
@@ -758,11 +805,59 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         x.out_conn = d_conn;
         x.out_hops = d_hops;
         apply_extras(x, ex);
-        // same counter block: next and finished restart at 0, the spill count
-        // ([2]) and the error / invalid flags carry over
-        FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 2 * sizeof(int), stream));
-        rc = pool_launch(x, c->p_grid, stream);
-        if (rc) return rc;
+        const int xgrid = c->p_grid;
+        auto issue = [&](unsigned evflags) -> int {
+            FC_CUDA_TRY(cudaMemsetAsync(c->qstat, 0, sizeof(QueryStat) * (size_t)nq, stream));
+            FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 8 * sizeof(int), stream));
+            int r = pool_launch(a, grid, stream);
+            if (r) return r;
+            FC_CUDA_TRY(cudaEventRecordWithFlags(c->evm, stream, evflags));
+            // same counter block: next and finished restart at 0, the spill
+            // count ([2]) and the error / invalid flags carry over
+            FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 2 * sizeof(int), stream));
+            return pool_launch(x, xgrid, stream);
+        };
+        if (o.use_graph) {
+            // the two launches and their resets as one CUDA graph, replayed
+            // while every argument (pointers, sizes, grids) stays the same
+            unsigned char key[sizeof(PoolArgs) * 2 + 3 * sizeof(int)];
+            std::memcpy(key, &a, sizeof(PoolArgs));
+            std::memcpy(key + sizeof(PoolArgs), &x, sizeof(PoolArgs));
+            int tail[3] = {grid, xgrid, nq};
+            std::memcpy(key + 2 * sizeof(PoolArgs), tail, sizeof(tail));
+            static_assert(sizeof(key) <= sizeof(c->gkey), "graph key too large");
+            if (!(c->gexec && c->gkey_len == sizeof(key) &&
+                  std::memcmp(c->gkey, key, sizeof(key)) == 0)) {
+                if (c->gexec) cudaGraphExecDestroy(c->gexec);
+                c->gexec = nullptr;
+                c->gkey_len = 0;
+                FC_CUDA_TRY(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                int r = issue(cudaEventRecordExternal);
+                cudaGraph_t g = nullptr;
+                cudaError_t e = cudaStreamEndCapture(stream, &g);
+                if (r || e != cudaSuccess) {
+                    if (g) cudaGraphDestroy(g);
+                    if (!r) fc_set_last_cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+                    return r ? r : FC_ERR_CUDA;
+                }
+                cudaGraphExec_t ge = nullptr;
+                e = cudaGraphInstantiate(&ge, g, 0);
+                cudaGraphDestroy(g);
+                FC_CUDA_TRY(e);
+                c->gexec = ge;
+                std::memcpy(c->gkey, key, sizeof(key));
+                c->gkey_len = sizeof(key);
+                ++c->graph_captures;
+                graph_use = 2;
+            } else {
+                ++c->graph_replays;
+                graph_use = 1;
+            }
+            FC_CUDA_TRY(cudaGraphLaunch(c->gexec, stream));
+        } else {
+            rc = issue(cudaEventRecordDefault);
+            if (rc) return rc;
+        }
         launches = 2;
     } else if (engine == FC_ENGINE_PERSISTENT) {
         PersistArgs a;
@@ -851,6 +946,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         }
         fill_stats(st, tot, launches);
         st->escalated = esc;
+        st->graph = graph_use;
         float ms = 0, m0 = 0, m1 = 0;
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);
         cudaEventElapsedTime(&m0, c->ev0, c->evm);

@@ -71,10 +71,21 @@ struct DevCtx {
     size_t tmp_q_cap = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evm = nullptr;
     cudaStream_t stream = nullptr;
-    // cached CUDA graph of the last batched launch
+    // cached CUDA graph of the last batched launch, keyed by its arguments
     cudaGraphExec_t gexec = nullptr;
-    unsigned long long gkey = 0;
+    unsigned char gkey[512];
+    size_t gkey_len = 0;
+    int graph_replays = 0;           // replays of the cached graph (tests)
+    int graph_captures = 0;          // captures made
+    int *selftest = nullptr;         // barrier + flag of the wait self-test
+    // staging of host-array batches (queries in, answers out)
+    int32_t *b_stage = nullptr;
+    size_t b_stage_cap = 0;
 };
+
+// Device staging for a host-array batch of n queries: 5n ints, kept between
+// calls so that repeated batches of the same size reuse a captured graph.
+int32_t *batch_staging(DevCtx *c, size_t n, int *rc);
 
 DevCtx *get_ctx(int *err);
 
@@ -98,6 +109,10 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
                        const int32_t *d_s, const int32_t *d_t, int32_t nq, int32_t *d_conn,
                        int32_t *d_hops, const fc_opts &o, fc_stats *st, cudaStream_t stream,
                        bool sync, const BatchExtras *ex = nullptr);
+
+// Bounded-wait self-test: one CTA waits at a two-CTA barrier until the wait
+// expires; returns FC_ERR_TIMEOUT when it did.
+int engine_selftest_wait(DevCtx *c, int timeout_ms, double *elapsed_ms, cudaStream_t stream);
 
 void set_error(const char *fmt, ...);
 

@@ -152,7 +152,8 @@ __device__ __forceinline__ uint8_t claim_u8(uint8_t *status, int v, uint8_t code
 constexpr unsigned long long BARRIER_TIMEOUT_NS = 2000000000ull;  // 2 s
 constexpr long long BARRIER_MAX_SPINS = 1ll << 25;
 
-__device__ __forceinline__ bool grid_barrier(int *bar, int *err, int nblocks)
+__device__ __forceinline__ bool grid_barrier(int *bar, int *err, int nblocks,
+                                             unsigned long long timeout_ns = BARRIER_TIMEOUT_NS)
 {
     __syncthreads();
     __shared__ int s_ok;
@@ -170,7 +171,7 @@ __device__ __forceinline__ bool grid_barrier(int *bar, int *err, int nblocks)
             long long spins = 0;
             while (ld_acquire_gpu(bar + 1) == gen) {
                 if (++spins > BARRIER_MAX_SPINS ||
-                    ((spins & 255) == 0 && global_timer_ns() - t0 > BARRIER_TIMEOUT_NS)) {
+                    ((spins & 255) == 0 && global_timer_ns() - t0 > timeout_ns)) {
                     atomicCAS(err, 0, FC_ERR_TIMEOUT);
                     ok = 0;
                     break;

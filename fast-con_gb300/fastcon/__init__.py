@@ -38,7 +38,7 @@ EXPORTS = [
     "fc_graph_info", "fc_graph_get_csr", "fc_graph_free", "fc_bfs_levels", "fc_bfs_levels_ex",
     "fc_stcon", "fc_stcon_ex", "fc_stcon_depth", "fc_stcon_batch", "fc_stcon_batch_device",
     "fc_stcon_batch_noalloc", "fc_sched_set_weights", "fc_sched_get_weights",
-    "fc_mlp_loss_grad", "fc_mlp_train", "fc_stcon_batch_scripted",
+    "fc_mlp_loss_grad", "fc_mlp_train", "fc_stcon_batch_scripted", "fc_selftest_wait",
     "fc_strerror", "fc_last_error_message", "fc_device_info", "fc_version",
 ]
 
@@ -62,7 +62,8 @@ class Stats(ctypes.Structure):
                 ("steps", ctypes.c_int32), ("bottom_up_steps", ctypes.c_int32),
                 ("gpu_ms", ctypes.c_double), ("alg_bytes", ctypes.c_int64),
                 ("escalated", ctypes.c_int32), ("launches", ctypes.c_int32),
-                ("kernel_ms", ctypes.c_double * 2), ("kernel_alg_bytes", ctypes.c_int64 * 2)]
+                ("kernel_ms", ctypes.c_double * 2), ("kernel_alg_bytes", ctypes.c_int64 * 2),
+                ("graph", ctypes.c_int32), ("pad_", ctypes.c_int32)]
 
     def as_dict(self):
         d = {}
@@ -114,6 +115,7 @@ def lib():
                                             _VP]),
             "fc_stcon_batch_scripted": (ctypes.c_int, [_VP, _VP, _VP, _I32, _VP, _I32, _VP, _VP,
                                                        _VP, _VP, _I32, _VP]),
+            "fc_selftest_wait": (ctypes.c_int, [_I32, _VP]),
             "fc_strerror": (ctypes.c_char_p, [ctypes.c_int]),
             "fc_last_error_message": (ctypes.c_char_p, []),
             "fc_device_info": (ctypes.c_int, [_VP, _VP, _VP, _VP]),
@@ -297,6 +299,13 @@ def stcon_batch_device(graphs, s_ptr, t_ptr, nq, conn_ptr, hops_ptr, graph_idx_p
                                        ctypes.byref(st) if stats else None),
            "fc_stcon_batch_device")
     return st.as_dict() if stats else None
+
+
+def selftest_wait(timeout_ms: int = 200):
+    """Run the bounded-wait self-test; returns (status code, kernel ms)."""
+    ms = np.zeros(1, np.float64)
+    rc = lib().fc_selftest_wait(int(timeout_ms), _P(ms))
+    return rc, float(ms[0])
 
 
 def device_info():

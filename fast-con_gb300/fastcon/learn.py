@@ -315,16 +315,25 @@ def main():
     t1 = time.time()
     nval = len(X) // 10
     w, curve = train(X[nval:], Y[nval:], epochs=args.epochs, SW=SW[nval:])
-    # second round: label the states the learned schedule itself visits
+    # second round: label the states the learned schedule itself visits; the
+    # validation rows of both rounds stay out of training
     set_weights(w)
     X2, Y2, SW2 = build_dataset(args.queries, states_per_graph=3000, seed=1,
                                 policies=(SCHED_LEARNED,))
-    X = np.concatenate([X, X2])
-    Y = np.concatenate([Y, Y2])
-    SW = np.concatenate([SW, SW2])
+    nval2 = len(X2) // 10
+    Xv = np.concatenate([X[:nval], X2[:nval2]])
+    Yv = np.concatenate([Y[:nval], Y2[:nval2]])
+    SWv = np.concatenate([SW[:nval], SW2[:nval2]])
+    X = np.concatenate([X[nval:], X2[nval2:]])
+    Y = np.concatenate([Y[nval:], Y2[nval2:]])
+    SW = np.concatenate([SW[nval:], SW2[nval2:]])
     perm = np.random.default_rng(2).permutation(len(X))
     X, Y, SW = X[perm], Y[perm], SW[perm]
-    w, curve = train(X[nval:], Y[nval:], epochs=args.epochs, SW=SW[nval:], w0=w)
+    w, curve = train(X, Y, epochs=args.epochs, SW=SW, w0=w)
+    nval = len(Xv)
+    X = np.concatenate([Xv, X])
+    Y = np.concatenate([Yv, Y])
+    SW = np.concatenate([SWv, SW])
     vloss, _ = loss_grad(X[:nval], Y[:nval], w, SW[:nval])
     # validation accuracy per head (host forward pass in float64)
     acc = head_accuracy(X[:nval], Y[:nval], w)

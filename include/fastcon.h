@@ -93,6 +93,10 @@ typedef struct fc_stats {
                                  [1] grid kernel for escalated queries       */
     int64_t kernel_alg_bytes[2]; /* alg_bytes of the queries each kernel
                                     finished (same split as kernel_ms)       */
+    int32_t graph;            /* batched with use_graph: 1 = replayed the
+                                 cached CUDA graph, 2 = captured a new one,
+                                 0 = direct launches                          */
+    int32_t pad_;
 } fc_stats;
 
 void fc_opts_init(fc_opts *o);
@@ -238,6 +242,16 @@ int fc_stcon_batch_noalloc(const int32_t *d_row_ptr, const int32_t *d_col, int32
                            const int32_t *d_rrow_ptr, const int32_t *d_rcol, const int32_t *d_s,
                            const int32_t *d_t, int32_t nq, int32_t *d_connected, int32_t *d_hops,
                            int32_t sched, void *stream);
+
+/* ---- failure detection ---------------------------------------------------- */
+/* Self-test of the bounded device-side waits every traversal kernel uses (no
+ * counterpart in the reference, whose grid barrier GlobalSync,
+ * BFS-4K/src/device/Util/GlobalSync.cu:12, spins without bound).  Launches one CTA into a grid barrier sized for two CTAs:
+ * nothing else arrives, so the wait expires after timeout_ms (1..2000) and
+ * the kernel returns with FC_ERR_TIMEOUT recorded.  Returns FC_ERR_TIMEOUT
+ * when the wait expired as designed (the device stays usable), FC_OK never,
+ * another code on failure; *elapsed_ms (nullable) gets the kernel's time. */
+int fc_selftest_wait(int32_t timeout_ms, double *elapsed_ms);
 
 /* ---- misc ---------------------------------------------------------------- */
 const char *fc_strerror(int code);

@@ -47,6 +47,8 @@ def test_status_codes_without_device(fastcon_lib):
     assert L.fc_bfs_levels(None, 0, None) == fastcon_lib.ERR_INVALID
     assert L.fc_graph_load_edgelist(b"/nonexistent/file.txt", -1, 0,
                                     ctypes.byref(h)) == fastcon_lib.ERR_IO
+    assert L.fc_selftest_wait(0, None) == fastcon_lib.ERR_INVALID
+    assert L.fc_selftest_wait(5000, None) == fastcon_lib.ERR_INVALID
     assert L.fc_version() == 100
 
 
@@ -54,3 +56,6 @@ def test_opts_layout(fastcon_lib):
     o = fastcon_lib.make_opts(sched=2, engine=3, block=256)
     assert (o.sched, o.engine, o.block) == (2, 3, 256)
     assert ctypes.sizeof(fastcon_lib.Opts) == 4 * 6 + 8 + 4 * 8
+    # fc_stats: 2 x int64, 2 x int32, double, int64, 2 x int32, 2 x double,
+    # 2 x int64, 2 x int32
+    assert ctypes.sizeof(fastcon_lib.Stats) == 16 + 8 + 8 + 8 + 8 + 16 + 16 + 8

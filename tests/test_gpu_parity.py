@@ -124,6 +124,27 @@ def test_er_stcon_matches_reference(fastcon_lib, er_graph, er_golden, engine, sc
             assert er_graph.stcon(s[k], t[k], o) == (want[k] >= 0, want[k])
 
 
+def test_batched_graph_replay(fastcon_lib, er_graph, er_golden):
+    """use_graph captures the batched launch once and replays it for the next
+    batch of the same size; the replay reads the new queries."""
+    fc = fastcon_lib
+    s, t = np.array(er_golden["s"]), np.array(er_golden["t"])
+    want = np.array(er_golden["hops"])
+    o = fc.make_opts(sched=fc.SCHED_HEURISTIC, engine=fc.ENGINE_BATCHED, use_graph=1)
+    conn, hops, st = fc.stcon_batch(er_graph, s, t, opts=o, stats=True)
+    assert (hops == want).all() and st["graph"] in (1, 2)
+    # reversed pairs: same distances on an undirected graph, replayed graph
+    conn, hops, st = fc.stcon_batch(er_graph, t, s, opts=o, stats=True)
+    assert (hops == want).all() and st["graph"] == 1
+    assert st["edges_inspected"] > 0 and st["kernel_ms"][0] > 0
+    # another size captures again; without use_graph nothing is captured
+    conn, hops, st = fc.stcon_batch(er_graph, s[:40], t[:40], opts=o, stats=True)
+    assert (hops == want[:40]).all() and st["graph"] == 2
+    o0 = fc.make_opts(sched=fc.SCHED_HEURISTIC, engine=fc.ENGINE_BATCHED)
+    conn, hops, st = fc.stcon_batch(er_graph, s, t, opts=o0, stats=True)
+    assert (hops == want).all() and st["graph"] == 0
+
+
 # --------------------------------------------------------------------------
 # the reference's known-answer run (Graph500 R-MAT scale 16)
 # --------------------------------------------------------------------------
