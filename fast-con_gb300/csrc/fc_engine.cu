@@ -129,9 +129,11 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
                 if (a.mlp) {  // every CTA computes the same decision
                     float f[MLP_IN], o[MLP_OUT];
                     ql_features(ql, f);
-                    mlp_forward_scalar(a.mlp, f, o);
-                    ql_apply_logits(ql, o, 1, bu_cap);
-                    if (a.force_variant >= 0) ql.variant = a.force_variant;
+                    if (mlp_in_box(a.mlp, f)) {
+                        mlp_forward_scalar(a.mlp, f, o);
+                        ql_apply_logits(ql, o, 1, bu_cap);
+                        if (a.force_variant >= 0) ql.variant = a.force_variant;
+                    }
                 }
             }
             __syncthreads();
@@ -347,9 +349,11 @@ static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, in
         if (learned) {
             float f[MLP_IN], o[MLP_OUT];
             ql_features(q, f);
-            mlp_forward_scalar(c->h_mlp, f, o);
-            ql_apply_logits(q, o, 1, bu_cap);
-            if (force_variant >= 0) q.variant = force_variant;
+            if (mlp_in_box(c->h_mlp, f)) {
+                mlp_forward_scalar(c->h_mlp, f, o);
+                ql_apply_logits(q, o, 1, bu_cap);
+                if (force_variant >= 0) q.variant = force_variant;
+            }
         }
         const int x = q.side;
         StepArgs a;

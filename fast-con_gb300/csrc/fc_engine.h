@@ -57,9 +57,10 @@ struct DevCtx {
     void *p_slots = nullptr;
     void *p_jobs = nullptr;
     int p_grid = 0;
-    // learned schedule weights (1,703 floats), device and host copies
+    // learned schedule weights (1,703 floats) and feature box (24 floats),
+    // device and host copies
     float *d_mlp = nullptr;
-    float h_mlp[1703];
+    float h_mlp[1727];
     int mlp_ready = 0;
     int b_log_cap = 0;
     int *b_ctr = nullptr;            // [0] next query, [1] spill count, [2] error

@@ -16,6 +16,7 @@
 //   k_adam       Adam update of the 1,703 parameters (Kingma & Ba, 2015).
 // softmax uses CUDA's expf / logf.
 #include <cmath>
+#include <cfloat>
 #include <cstring>
 #include <vector>
 
@@ -128,12 +129,21 @@ static int mlp_grid(int n)
     return g < 1 ? 1 : g;
 }
 
-int set_mlp_weights(DevCtx *c, const float *w)
+// n = MLP_PARAMS (no feature box: the network is always consulted) or
+// MLP_STORE (parameters followed by the box lo[12], hi[12]).
+int set_mlp_weights(DevCtx *c, const float *w, int n)
 {
-    if (!c->d_mlp) FC_CUDA_TRY(cudaMalloc(&c->d_mlp, sizeof(float) * MLP_PARAMS));
-    FC_CUDA_TRY(cudaMemcpy(c->d_mlp, w, sizeof(float) * MLP_PARAMS, cudaMemcpyHostToDevice));
+    static_assert(sizeof(c->h_mlp) == sizeof(float) * MLP_STORE, "weight store size");
+    float h[MLP_STORE];
+    std::memcpy(h, w, sizeof(float) * MLP_PARAMS);
+    for (int i = 0; i < MLP_IN; ++i) {
+        h[MLP_BOX + i] = n == MLP_STORE ? w[MLP_BOX + i] : -FLT_MAX;
+        h[MLP_BOX + MLP_IN + i] = n == MLP_STORE ? w[MLP_BOX + MLP_IN + i] : FLT_MAX;
+    }
+    if (!c->d_mlp) FC_CUDA_TRY(cudaMalloc(&c->d_mlp, sizeof(float) * MLP_STORE));
+    FC_CUDA_TRY(cudaMemcpy(c->d_mlp, h, sizeof(float) * MLP_STORE, cudaMemcpyHostToDevice));
     FC_CUDA_TRY(cudaDeviceSynchronize());  // read by kernels on non-blocking streams
-    std::memcpy(c->h_mlp, w, sizeof(float) * MLP_PARAMS);
+    std::memcpy(c->h_mlp, h, sizeof(float) * MLP_STORE);
     c->mlp_ready = 1;
     return FC_OK;
 }
@@ -144,20 +154,20 @@ using namespace fc;
 
 extern "C" int fc_sched_set_weights(const float *w, int32_t n)
 {
-    if (!w || n != MLP_PARAMS) {
-        set_error("fc_sched_set_weights: expected %d floats", MLP_PARAMS);
+    if (!w || (n != MLP_PARAMS && n != MLP_STORE)) {
+        set_error("fc_sched_set_weights: expected %d or %d floats", MLP_PARAMS, MLP_STORE);
         return FC_ERR_INVALID;
     }
     int rc = FC_OK;
     DevCtx *c = get_ctx(&rc);
     if (!c) return rc;
     std::lock_guard<std::mutex> lk(c->mu);
-    return set_mlp_weights(c, w);
+    return set_mlp_weights(c, w, n);
 }
 
 extern "C" int fc_sched_get_weights(float *w, int32_t n)
 {
-    if (!w || n != MLP_PARAMS) return FC_ERR_INVALID;
+    if (!w || (n != MLP_PARAMS && n != MLP_STORE)) return FC_ERR_INVALID;
     int rc = FC_OK;
     DevCtx *c = get_ctx(&rc);
     if (!c) return rc;
@@ -166,7 +176,7 @@ extern "C" int fc_sched_get_weights(float *w, int32_t n)
         set_error("no weights loaded");
         return FC_ERR_INVALID;
     }
-    std::memcpy(w, c->h_mlp, sizeof(float) * MLP_PARAMS);
+    std::memcpy(w, c->h_mlp, sizeof(float) * (size_t)n);
     return FC_OK;
 }
 

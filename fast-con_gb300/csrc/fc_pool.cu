@@ -417,7 +417,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             if (track) {
                 float f[MLP_IN];
                 ql_features(sm.ql, f);
-                if (a.sched == FC_SCHED_LEARNED && a.mlp) {
+                if (a.sched == FC_SCHED_LEARNED && a.mlp && mlp_in_box(a.mlp, f)) {
                     float o[MLP_OUT];
                     mlp_forward_warp(a.mlp, f, o);
                     if (tid == 0) {

@@ -182,21 +182,27 @@ __host__ __device__ inline void ql_update_hist(QLocal &q, int x, const unsigned 
 }
 
 // ---------------------------------------------------------------------------
-// Learned schedule.  Twelve features per decision (all from integer counters):
-//   0,1  log2(1 + frontier vertices) / 24 of side 0, side 1
-//   2,3  log2(1 + frontier adjacency entries) / 32 of side 0, side 1
-//   4    unexplored fraction: adjacency entries of unclaimed vertices / ne
-//   5    side expanded last (0 or 1; 0.5 before the first step)
-//   6-8  side 0 frontier degree histogram (< 8, < 128, >= 128), fractions
-//   9-11 side 1 frontier degree histogram, fractions
+// Learned schedule.  Twelve features per decision (all from integer counters,
+// scaled so that graphs of different sizes give comparable values):
+//   0,1   log2(1 + frontier vertices) / log2(2 + nv), side 0 and side 1
+//   2,3   log2(1 + frontier adjacency entries) / log2(2 + ne), sides 0 and 1
+//   4     unexplored fraction: adjacency entries of unclaimed vertices / ne
+//   5     side expanded last (0 or 1; 0.5 before the first step)
+//   6,7   side 0 frontier: fraction of degree < 8, fraction of degree >= 128
+//   8,9   side 1 frontier: the same
+//   10,11 log2(1 + radius) / 8 of side 0, side 1 (levels expanded so far)
 // MLP 12 -> 32 (ReLU) -> 32 (ReLU) -> 7 logits: side (2), direction (2),
 // expansion variant (3).  1,703 float parameters in this order:
-//   W1[32][12], b1[32], W2[32][32], b2[32], W3[7][32], b3[7].
+//   W1[32][12], b1[32], W2[32][32], b2[32], W3[7][32], b3[7];
+// optionally followed by the feature box of the training data, lo[12] and
+// hi[12]: outside the box the network is not consulted (the heuristic
+// decides), so graphs unlike the training graphs fall back to the heuristic.
 // ---------------------------------------------------------------------------
 constexpr int MLP_IN = 12, MLP_H = 32, MLP_OUT = 7;
 constexpr int MLP_W1 = 0, MLP_B1 = MLP_W1 + MLP_H * MLP_IN, MLP_W2 = MLP_B1 + MLP_H,
               MLP_B2 = MLP_W2 + MLP_H * MLP_H, MLP_W3 = MLP_B2 + MLP_H,
               MLP_B3 = MLP_W3 + MLP_OUT * MLP_H, MLP_PARAMS = MLP_B3 + MLP_OUT;
+constexpr int MLP_BOX = MLP_PARAMS, MLP_STORE = MLP_PARAMS + 2 * MLP_IN;
 static_assert(MLP_PARAMS == 1703, "parameter count");
 
 __host__ __device__ inline void ql_features(const QLocal &q, float *f)
@@ -205,10 +211,11 @@ __host__ __device__ inline void ql_features(const QLocal &q, float *f)
     const double m0 = (double)(q.dt[0] - q.dh[0]), m1 = (double)(q.dt[1] - q.dh[1]);
     long long un = q.ne - (long long)(q.dt[0] + q.dt[1]);
     if (un < 0) un = 0;
-    f[0] = (float)(log2(1.0 + n0) / 24.0);
-    f[1] = (float)(log2(1.0 + n1) / 24.0);
-    f[2] = (float)(log2(1.0 + m0) / 32.0);
-    f[3] = (float)(log2(1.0 + m1) / 32.0);
+    const double lv = log2(2.0 + (double)q.nv), le = log2(2.0 + (double)q.ne);
+    f[0] = (float)(log2(1.0 + n0) / lv);
+    f[1] = (float)(log2(1.0 + n1) / lv);
+    f[2] = (float)(log2(1.0 + m0) / le);
+    f[3] = (float)(log2(1.0 + m1) / le);
     f[4] = q.ne > 0 ? (float)((double)un / (double)q.ne) : 0.f;
     f[5] = q.last_side < 0 ? 0.5f : (float)q.last_side;
     for (int x = 0; x < 2; ++x) {
@@ -217,8 +224,19 @@ __host__ __device__ inline void ql_features(const QLocal &q, float *f)
             h[b] = (double)(q.ht[x][b] - q.hh[x][b]);
             tot += h[b];
         }
-        for (int b = 0; b < 3; ++b) f[6 + 3 * x + b] = tot > 0 ? (float)(h[b] / tot) : 0.f;
+        f[6 + 2 * x] = tot > 0 ? (float)(h[0] / tot) : 0.f;
+        f[7 + 2 * x] = tot > 0 ? (float)(h[2] / tot) : 0.f;
+        f[10 + x] = (float)(log2(1.0 + (double)q.radius[x]) / 8.0);
     }
+}
+
+// True when every feature lies inside the training box (W[MLP_BOX..]).
+__host__ __device__ inline bool mlp_in_box(const float *W, const float *f)
+{
+    bool in = true;
+    for (int i = 0; i < MLP_IN; ++i)
+        in = in && f[i] >= W[MLP_BOX + i] && f[i] <= W[MLP_BOX + MLP_IN + i];
+    return in;
 }
 
 // Forward pass by one thread (host-loop engine on the host, grid engine on
@@ -267,10 +285,10 @@ __device__ __forceinline__ void mlp_forward_warp(const float *__restrict__ W, co
 }
 
 // Turn logits into the step, within the engine's constraints (one side only
-// for BFS, bottom-up only where allowed).  The side and direction heads
-// override the heuristic's choice (already in q) only when confident: a logit
-// margin above MLP_MARGIN (softmax probability above 0.75); otherwise the
-// fixed-threshold heuristic stands.  The variant head always decides.
+// for BFS, bottom-up only where allowed).  Each head overrides the
+// heuristic's choice (already in q) only when confident: a logit margin above
+// MLP_MARGIN over every other class (softmax probability above 0.75 for two
+// classes); otherwise the fixed-threshold heuristic stands.
 constexpr float MLP_MARGIN = 1.0986f;  // ln 3
 
 __host__ __device__ inline void ql_apply_logits(QLocal &q, const float *o, int allow_bu,
@@ -291,7 +309,10 @@ __host__ __device__ inline void ql_apply_logits(QLocal &q, const float *o, int a
     int v = 0;
     if (o[5] > o[4 + v]) v = 1;
     if (o[6] > o[4 + v]) v = 2;
-    q.variant = v;
+    float second = -3.0e38f;
+    for (int k = 0; k < 3; ++k)
+        if (k != v && o[4 + k] > second) second = o[4 + k];
+    if (o[4 + v] - second > MLP_MARGIN) q.variant = v;
 }
 
 // Scripted action byte: bit 0 side, bit 1 bottom-up, bits 2-3 variant + 1

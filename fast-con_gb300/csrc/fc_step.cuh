@@ -24,6 +24,7 @@
 namespace fc {
 
 constexpr int GATHER_PER_THREAD = 4;
+constexpr int BU_GROUP = 4;  // bottom-up: neighbours loaded together
 
 struct AppendTarget {
     int32_t *log;       // log base of the slot
@@ -408,15 +409,28 @@ struct BottomUpSTCON {
         bool unvisited = s == ST_UNVISITED;
         if (!unvisited && s != other_front) return -1;
         int b = __ldg(row_ptr + v), e = __ldg(row_ptr + v + 1);
-        for (int j = b; j < e; ++j) {
-            ++inspected;
-            if (ld_cg_u8(status + __ldg(col + j)) == front_code) {
-                if (unvisited) {
-                    status[v] = next_code;
-                    return v;
+        // neighbours in groups of BU_GROUP: the group's column and status
+        // loads are independent and overlap; the first hit in row order
+        // decides, and only the neighbours up to it count as inspected
+        for (int j = b; j < e; j += BU_GROUP) {
+            int u[BU_GROUP];
+            uint8_t su[BU_GROUP];
+#pragma unroll
+            for (int k = 0; k < BU_GROUP; ++k) u[k] = j + k < e ? __ldg(col + j + k) : -1;
+#pragma unroll
+            for (int k = 0; k < BU_GROUP; ++k) su[k] = u[k] >= 0 ? ld_cg_u8(status + u[k]) : 0;
+#pragma unroll
+            for (int k = 0; k < BU_GROUP; ++k) {
+                if (u[k] < 0) break;
+                ++inspected;
+                if (su[k] == front_code) {
+                    if (unvisited) {
+                        status[v] = next_code;
+                        return v;
+                    }
+                    *(volatile int *)found = 1;
+                    return -1;
                 }
-                *(volatile int *)found = 1;
-                return -1;
             }
         }
         return -1;
@@ -431,11 +445,20 @@ struct BottomUpBFS {
     {
         if (ld_cg(levels + v) >= 0) return -1;
         int b = __ldg(row_ptr + v), e = __ldg(row_ptr + v + 1);
-        for (int j = b; j < e; ++j) {
-            ++inspected;
-            if (ld_cg(levels + __ldg(col + j)) == level) {
-                levels[v] = level + 1;
-                return v;
+        for (int j = b; j < e; j += BU_GROUP) {
+            int u[BU_GROUP], lu[BU_GROUP];
+#pragma unroll
+            for (int k = 0; k < BU_GROUP; ++k) u[k] = j + k < e ? __ldg(col + j + k) : -1;
+#pragma unroll
+            for (int k = 0; k < BU_GROUP; ++k) lu[k] = u[k] >= 0 ? ld_cg(levels + u[k]) : -1;
+#pragma unroll
+            for (int k = 0; k < BU_GROUP; ++k) {
+                if (u[k] < 0) break;
+                ++inspected;
+                if (lu[k] == level) {
+                    levels[v] = level + 1;
+                    return v;
+                }
             }
         }
         return -1;

@@ -53,15 +53,26 @@ def init_weights(seed: int = 0) -> np.ndarray:
     return w
 
 
-def set_weights(w: np.ndarray) -> None:
-    w = np.ascontiguousarray(w, dtype=np.float32)
+def set_weights(w: np.ndarray, box=None) -> None:
+    """Install weights; `box` = (lo[12], hi[12]) limits the network to steps
+    whose features lie inside the training data's range."""
+    w = np.asarray(w, dtype=np.float32).ravel()
+    if box is not None:
+        w = np.concatenate([w, np.asarray(box[0], np.float32), np.asarray(box[1], np.float32)])
+    w = np.ascontiguousarray(w)
     _check(lib().fc_sched_set_weights(ctypes.c_void_p(w.ctypes.data), w.size),
            "fc_sched_set_weights")
 
 
+def feature_box(X, margin=0.02):
+    """Per-feature range of the training states, widened by `margin`."""
+    return (X.min(axis=0) - margin).astype(np.float32), (X.max(axis=0) + margin).astype(np.float32)
+
+
 def load_default_weights(path: str = WEIGHTS_PATH) -> dict:
     d = json.load(open(path))
-    set_weights(np.array(d["weights"], dtype=np.float32))
+    box = (d["box"]["lo"], d["box"]["hi"]) if "box" in d else None
+    set_weights(np.array(d["weights"], dtype=np.float32), box)
     return d
 
 
@@ -315,9 +326,10 @@ def main():
     t1 = time.time()
     nval = len(X) // 10
     w, curve = train(X[nval:], Y[nval:], epochs=args.epochs, SW=SW[nval:])
+    box = feature_box(X[nval:])
     # second round: label the states the learned schedule itself visits; the
     # validation rows of both rounds stay out of training
-    set_weights(w)
+    set_weights(w, box)
     X2, Y2, SW2 = build_dataset(args.queries, states_per_graph=3000, seed=1,
                                 policies=(SCHED_LEARNED,))
     nval2 = len(X2) // 10
@@ -330,6 +342,7 @@ def main():
     perm = np.random.default_rng(2).permutation(len(X))
     X, Y, SW = X[perm], Y[perm], SW[perm]
     w, curve = train(X, Y, epochs=args.epochs, SW=SW, w0=w)
+    box = feature_box(X)
     nval = len(Xv)
     X = np.concatenate([Xv, X])
     Y = np.concatenate([Yv, Y])
@@ -339,7 +352,7 @@ def main():
     acc = head_accuracy(X[:nval], Y[:nval], w)
     acc_heur = heuristic_accuracy(X[:nval], Y[:nval])
     t2 = time.time()
-    set_weights(w)
+    set_weights(w, box)
     ev = {}
     G = Graph.rmat(24, 8 << 24, seed=9, perm_seed=9)
     rp, _ = G.csr_row_ptr()
@@ -356,6 +369,7 @@ def main():
     G.free()
     meta = {
         "weights": [float(x) for x in w],
+        "box": {"lo": [float(x) for x in box[0]], "hi": [float(x) for x in box[1]]},
         "layout": "W1[32][12] b1[32] W2[32][32] b2[32] W3[7][32] b3[7]",
         "training": {"graphs": "R-MAT scale 18-22 x2, seeds 1000-1009", "queries": args.queries,
                      "samples": int(len(X) - nval), "validation": int(nval),

@@ -190,11 +190,15 @@ int fc_stcon_batch_device(fc_graph *const *gs, int32_t ngraphs, const int32_t *d
 
 /* ---- learned schedule (no counterpart in the reference) ------------------ */
 
-/* Install the MLP weights of FC_SCHED_LEARNED for the current device: 1,703
- * floats, W1[32][12] b1[32] W2[32][32] b2[32] W3[7][32] b3[7]; logits 0-1
- * pick the side, 2-3 top-down / bottom-up, 4-6 the expansion variant.  The
- * network reads 12 features per step (frontier sizes and adjacency sums of
- * both sides, unexplored fraction, last side, frontier degree histograms). */
+/* Install the MLP weights of FC_SCHED_LEARNED for the current device: n =
+ * 1,703 floats, W1[32][12] b1[32] W2[32][32] b2[32] W3[7][32] b3[7], or
+ * 1,727 = those followed by the training feature box lo[12], hi[12] (steps
+ * whose features fall outside it are left to the heuristic).  Logits 0-1
+ * pick the side, 2-3 top-down / bottom-up, 4-6 the expansion variant; a head
+ * overrides the heuristic only with a logit margin above ln 3.  The network
+ * reads 12 features per step (frontier sizes and adjacency sums of both
+ * sides scaled by the graph size, unexplored fraction, last side, frontier
+ * degree mix, radii).  fc_sched_get_weights copies n (1,703 or 1,727). */
 int fc_sched_set_weights(const float *w, int32_t n);
 int fc_sched_get_weights(float *w, int32_t n);
 

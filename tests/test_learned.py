@@ -173,3 +173,42 @@ def test_trained_weights_beat_plain(fastcon_lib, oracle_mod):
     res = learn.evaluate(G, s, t, want, reps=1)
     assert res["learned"]["exact"] and res["plain"]["exact"] and res["heuristic"]["exact"]
     assert res["learned"]["edges_inspected"] < res["plain"]["edges_inspected"]
+
+
+def test_box_gate_and_margin(fastcon_lib, oracle_mod):
+    """The network steers only inside its feature box and only with a clear
+    logit margin; otherwise every decision is the heuristic's."""
+    fc = fastcon_lib
+    from fastcon import learn
+    u, v = graphs.rmat_edges(14, 8 << 14, seed=91, perm_seed=92)
+    G = fc.Graph.from_edges(u, v, 1 << 14)
+    rp, col = oracle_mod.build_csr(1 << 14, u, v)
+    s, t = graphs.pairs_with_degree(np.diff(rp), 300, seed=93)
+    _, want, _ = oracle_mod.stcon_batch(rp, col, s, t, nthreads=4)
+
+    def trace(sched):
+        hops, _, rec = learn.run_scripted(G, s, t, sched=sched, trace=True)
+        assert (hops == want).all()
+        d = learn.decode(rec)
+        order = np.lexsort((d["step"], d["q"]))
+        return d["q"][order], d["step"][order], d["side"][order], d["dir"][order]
+
+    heur = trace(fc.SCHED_HEURISTIC)
+    w = np.zeros(1703, np.float32)
+    w[1696 + 1] = 10.0  # side-1 logit: always expand t's side, with a clear margin
+    full = (np.full(12, -1e9), np.full(12, 1e9))
+    learn.set_weights(w, full)
+    q, step, side, _ = trace(fc.SCHED_LEARNED)
+    two = s[q] != t[q]
+    assert two.any() and (side[two] == 1).all()
+    # an empty box: the heuristic decides every step
+    learn.set_weights(w, (np.ones(12), np.zeros(12)))
+    got = trace(fc.SCHED_LEARNED)
+    for a, b in zip(got, heur):
+        assert (a == b).all()
+    # a margin below ln 3: the heuristic decides as well
+    w[1696 + 1] = 0.5
+    learn.set_weights(w, full)
+    got = trace(fc.SCHED_LEARNED)
+    for a, b in zip(got, heur):
+        assert (a == b).all()
