@@ -544,7 +544,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
 }
 
 template <int T>
-__global__ void __launch_bounds__(T) k_pool(PoolArgs a)
+__global__ void __launch_bounds__(T, 4) k_pool(PoolArgs a)
 {
     __shared__ SmemPool<T> sm;
     const int tid = threadIdx.x;

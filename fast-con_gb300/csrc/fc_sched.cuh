@@ -207,26 +207,28 @@ static_assert(MLP_PARAMS == 1703, "parameter count");
 
 __host__ __device__ inline void ql_features(const QLocal &q, float *f)
 {
-    const double n0 = (double)(q.tail[0] - q.head[0]), n1 = (double)(q.tail[1] - q.head[1]);
-    const double m0 = (double)(q.dt[0] - q.dh[0]), m1 = (double)(q.dt[1] - q.dh[1]);
+    // single precision throughout: FP64 is slow on this part and the
+    // features need no more than float resolution
+    const float n0 = (float)(q.tail[0] - q.head[0]), n1 = (float)(q.tail[1] - q.head[1]);
+    const float m0 = (float)(q.dt[0] - q.dh[0]), m1 = (float)(q.dt[1] - q.dh[1]);
     long long un = q.ne - (long long)(q.dt[0] + q.dt[1]);
     if (un < 0) un = 0;
-    const double lv = log2(2.0 + (double)q.nv), le = log2(2.0 + (double)q.ne);
-    f[0] = (float)(log2(1.0 + n0) / lv);
-    f[1] = (float)(log2(1.0 + n1) / lv);
-    f[2] = (float)(log2(1.0 + m0) / le);
-    f[3] = (float)(log2(1.0 + m1) / le);
-    f[4] = q.ne > 0 ? (float)((double)un / (double)q.ne) : 0.f;
+    const float lv = 1.f / log2f(2.f + (float)q.nv), le = 1.f / log2f(2.f + (float)q.ne);
+    f[0] = log2f(1.f + n0) * lv;
+    f[1] = log2f(1.f + n1) * lv;
+    f[2] = log2f(1.f + m0) * le;
+    f[3] = log2f(1.f + m1) * le;
+    f[4] = q.ne > 0 ? (float)un / (float)q.ne : 0.f;
     f[5] = q.last_side < 0 ? 0.5f : (float)q.last_side;
     for (int x = 0; x < 2; ++x) {
-        double h[3], tot = 0;
+        float h[3], tot = 0.f;
         for (int b = 0; b < 3; ++b) {
-            h[b] = (double)(q.ht[x][b] - q.hh[x][b]);
+            h[b] = (float)(q.ht[x][b] - q.hh[x][b]);
             tot += h[b];
         }
-        f[6 + 2 * x] = tot > 0 ? (float)(h[0] / tot) : 0.f;
-        f[7 + 2 * x] = tot > 0 ? (float)(h[2] / tot) : 0.f;
-        f[10 + x] = (float)(log2(1.0 + (double)q.radius[x]) / 8.0);
+        f[6 + 2 * x] = tot > 0.f ? h[0] / tot : 0.f;
+        f[7 + 2 * x] = tot > 0.f ? h[2] / tot : 0.f;
+        f[10 + x] = log2f(1.f + (float)q.radius[x]) * 0.125f;
     }
 }
 

@@ -90,17 +90,20 @@ __device__ __forceinline__ void warp_append(const int (&c)[K], const AppendTarge
 }
 
 // ---------------------------------------------------------------------------
-// Visitors: what happens at one neighbour v of a frontier vertex.
-// visit() returns v when this thread claimed it, else -1.
+// Visitors: what happens at one neighbour v of a frontier vertex, in two
+// phases so that a thread can have several neighbours' loads in flight:
+// probe(v) reads v's state; settle(v, probed) claims v when it was free and
+// returns v when this thread claimed it, else -1.  visit() = both.
 // ---------------------------------------------------------------------------
 struct VisitSTCON {
     uint8_t *status;
     uint8_t next_code;  // st_code(side, level + 1)
     int side;
     int *found;
-    __device__ __forceinline__ int visit(int v) const
+    __device__ __forceinline__ int probe(int v) const { return ld_cg_u8(status + v); }
+    __device__ __forceinline__ int settle(int v, int probed) const
     {
-        uint8_t s = ld_cg_u8(status + v);
+        uint8_t s = (uint8_t)probed;
         if (s == ST_UNVISITED) {
             s = claim_u8(status, v, next_code);
             if (s == ST_UNVISITED) return v;
@@ -108,17 +111,32 @@ struct VisitSTCON {
         if ((int)(s >> 7) != side) *(volatile int *)found = 1;
         return -1;
     }
+    __device__ __forceinline__ int visit(int v) const { return settle(v, probe(v)); }
 };
 
 struct VisitBFS {
     int32_t *levels;
     int32_t next_level;
-    __device__ __forceinline__ int visit(int v) const
+    __device__ __forceinline__ int probe(int v) const { return ld_cg(levels + v); }
+    __device__ __forceinline__ int settle(int v, int probed) const
     {
-        if (ld_cg(levels + v) >= 0) return -1;
+        if (probed >= 0) return -1;
         return atomicCAS(levels + v, -1, next_level) == -1 ? v : -1;
     }
+    __device__ __forceinline__ int visit(int v) const { return settle(v, probe(v)); }
 };
+
+// K neighbours at once: all K probes are issued before the first claim.
+// v[k] < 0 marks an empty entry (c[k] = -1).
+template <int K, class Vis>
+__device__ __forceinline__ void visit_k(const Vis &vis, const int (&v)[K], int (&c)[K])
+{
+    int p[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) p[k] = v[k] >= 0 ? vis.probe(v[k]) : 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) c[k] = v[k] >= 0 ? vis.settle(v[k], p[k]) : -1;
+}
 
 // ---------------------------------------------------------------------------
 // Walk col[b, e) with `nlanes` threads (lane_idx in [0, nlanes)); every warp
@@ -145,14 +163,15 @@ __device__ __forceinline__ void walk_range(const int32_t *__restrict__ col, int 
     const int k_end = z >> 2;
     for (int k0 = a >> 2; k0 < k_end; k0 += nlanes) {
         int k = k0 + lane_idx;
-        int c[4] = {-1, -1, -1, -1};
+        int v[4] = {-1, -1, -1, -1}, c[4];
         if (k < k_end) {
             int4 x = __ldg(col4 + k);
-            c[0] = vis.visit(x.x);
-            c[1] = vis.visit(x.y);
-            c[2] = vis.visit(x.z);
-            c[3] = vis.visit(x.w);
+            v[0] = x.x;
+            v[1] = x.y;
+            v[2] = x.z;
+            v[3] = x.w;
         }
+        visit_k<4>(vis, v, c);
         warp_append<4>(c, app);
     }
 }
@@ -242,13 +261,16 @@ __device__ __forceinline__ void expand_rows(const int32_t *__restrict__ col, int
         int lo = max(off, chunk), hi = min(off + d, chunk + G);
         for (int j = lo; j < hi; ++j) sm.gather[j - chunk] = rb + (j - off);
         __syncthreads();
-        int cnt = min(G, total - chunk);
-        for (int k0 = 0; k0 < cnt; k0 += T) {
-            int k = k0 + tid;
-            int c[1] = {-1};
-            if (k < cnt) c[0] = vis.visit(__ldg(col + sm.gather[k]));
-            warp_append<1>(c, app);
+        const int cnt = min(G, total - chunk);
+        // GATHER_PER_THREAD entries per thread, all loads in flight together
+        int v[GATHER_PER_THREAD], c[GATHER_PER_THREAD];
+#pragma unroll
+        for (int j = 0; j < GATHER_PER_THREAD; ++j) {
+            const int k = j * T + tid;
+            v[j] = k < cnt ? __ldg(col + sm.gather[k]) : -1;
         }
+        visit_k<GATHER_PER_THREAD>(vis, v, c);
+        warp_append<GATHER_PER_THREAD>(c, app);
         __syncthreads();
     }
 }
