@@ -374,12 +374,13 @@ def run_fastcon(args, cfg):
     value = total_q / (ms / 1000.0)
 
     # per-kernel split and algorithmic bytes (same workload, statistics on)
-    kms, kbytes, ins, esc, launches = np.zeros(2), np.zeros(2), 0, 0, 0
+    kms, kbytes, ins, esc, launches, vadj = np.zeros(2), np.zeros(2), 0, 0, 0, 0
     for _ in range(args.steps):
         st = step(stats=True)
         kms += np.array(st["kernel_ms"])
         kbytes += np.array(st["kernel_alg_bytes"])
         ins += st["edges_inspected"]
+        vadj += st["visited_adjacency"]
         esc = st["escalated"]
         launches = st["launches"]
     kms /= args.steps
@@ -464,6 +465,9 @@ def run_fastcon(args, cfg):
                            sched=args.sched, parallelism=f"replicas{ws}"),
             "exact": exact,
             "gteps_inspected": ins / args.steps / (ms / args.steps / 1000.0) / 1e9,
+            # the reference's TEPS numerator (count_visited_edges): edges of the
+            # visited vertices counted once, i.e. half their degree sum
+            "gteps_graph500": vadj / 2 / args.steps / (ms / args.steps / 1000.0) / 1e9,
             "edges_inspected_per_step": ins / args.steps,
             "plain": plain, "one_launch_per_query": single,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,

@@ -398,6 +398,7 @@ static void fill_stats(fc_stats *st, const QLocal &q, int launches)
     st->bottom_up_steps = q.bu_steps;
     st->alg_bytes = (int64_t)q.alg_bytes;
     st->launches = launches;
+    st->visited_adjacency = (int64_t)(q.dt[0] + q.dt[1]);
 }
 
 static void accumulate(QLocal &tot, const QueryStat &h)
@@ -405,6 +406,7 @@ static void accumulate(QLocal &tot, const QueryStat &h)
     tot.inspected += (unsigned long long)h.inspected;
     tot.alg_bytes += (unsigned long long)h.alg_bytes;
     tot.tail[0] += h.visited;
+    tot.dt[0] += (unsigned long long)h.visited_deg;
     tot.steps += h.steps;
     tot.bu_steps += h.bu_steps;
 }
@@ -912,6 +914,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
             tot.inspected += q.inspected;
             tot.alg_bytes += q.alg_bytes;
             tot.tail[0] += q.tail[0] + q.tail[1];
+            tot.dt[0] += q.dt[0] + q.dt[1];
             tot.steps += q.steps;
             tot.bu_steps += q.bu_steps;
         }

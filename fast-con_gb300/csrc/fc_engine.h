@@ -32,6 +32,7 @@ struct QueryStat {
     int bu_steps;
     int visited;
     int escalated;
+    long long visited_deg;  // degree sum of the claimed vertices
 };
 
 // Per-device context: workspaces grown on demand, events, the batched arena.

@@ -439,6 +439,7 @@ __device__ __forceinline__ void write_result(int q, const QLocal &ql, int32_t *o
         r.steps = ql.steps;
         r.bu_steps = ql.bu_steps;
         r.visited = ql.tail[0] + ql.tail[1];
+        r.visited_deg = (long long)(ql.dt[0] + ql.dt[1]);
         r.escalated = escalated;
         if (escalated) {
             // the persistent engine rewrites the record; keep the CTA's part

@@ -63,7 +63,8 @@ class Stats(ctypes.Structure):
                 ("gpu_ms", ctypes.c_double), ("alg_bytes", ctypes.c_int64),
                 ("escalated", ctypes.c_int32), ("launches", ctypes.c_int32),
                 ("kernel_ms", ctypes.c_double * 2), ("kernel_alg_bytes", ctypes.c_int64 * 2),
-                ("graph", ctypes.c_int32), ("pad_", ctypes.c_int32)]
+                ("graph", ctypes.c_int32), ("pad_", ctypes.c_int32),
+                ("visited_adjacency", ctypes.c_int64)]
 
     def as_dict(self):
         d = {}

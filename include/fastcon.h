@@ -97,6 +97,10 @@ typedef struct fc_stats {
                                  cached CUDA graph, 2 = captured a new one,
                                  0 = direct launches                          */
     int32_t pad_;
+    int64_t visited_adjacency; /* adjacency entries of the claimed vertices
+                                  (their degree sum); half of it is the
+                                  reference's TEPS numerator count_visited_edges
+                                  (S/adj_func.c:334-357) on a symmetric graph  */
 } fc_stats;
 
 void fc_opts_init(fc_opts *o);

@@ -57,5 +57,5 @@ def test_opts_layout(fastcon_lib):
     assert (o.sched, o.engine, o.block) == (2, 3, 256)
     assert ctypes.sizeof(fastcon_lib.Opts) == 4 * 6 + 8 + 4 * 8
     # fc_stats: 2 x int64, 2 x int32, double, int64, 2 x int32, 2 x double,
-    # 2 x int64, 2 x int32
-    assert ctypes.sizeof(fastcon_lib.Stats) == 16 + 8 + 8 + 8 + 8 + 16 + 16 + 8
+    # 2 x int64, 2 x int32, int64
+    assert ctypes.sizeof(fastcon_lib.Stats) == 16 + 8 + 8 + 8 + 8 + 16 + 16 + 8 + 8
