@@ -37,8 +37,9 @@ namespace fc {
 
 constexpr int POOL_TILE_V = 8192;    // vertices per bottom-up tile
 constexpr int POOL_TILE_R = 8192;    // log entries per reset tile
-constexpr int POOL_SPLIT_E = 8192;   // row-job length
-constexpr int POOL_JOBS = 4096;      // row jobs per slot and step
+constexpr int POOL_SPLIT_E = 4096;   // row-job length
+constexpr int POOL_JOBS = 16384;     // row jobs per slot and step
+constexpr int POOL_TILE_E = 16384;   // top-down: aim for about this many entries per tile
 constexpr unsigned long long PK_MASK = (1ull << 22) - 1;
 constexpr unsigned long long POOL_IDLE_NS = 4000000000ull;  // 4 s without progress
 
@@ -63,7 +64,7 @@ struct RowJob {
 // Step description: written by the owner before it publishes the step.
 struct PoolDesc {
     int q, gidx, mode, side, dir, level, other_radius, F, front_off, nvt, cap, nreset, variant;
-    int tile_mult;  // top-down tiles hold tile_mult chunks of T frontier vertices
+    int tile_v;     // top-down: frontier vertices per tile (< T, or a multiple of T)
     int track_hist; // count claimed vertices per degree bin (learned schedule)
     uint8_t *status;
     int32_t *levels;
@@ -196,12 +197,12 @@ __device__ void pool_tile(const PoolArgs &a, PoolSlot *slot, int tile, unsigned 
     }
     if (d.dir == DIR_TD) {
         SlotSink sink{slot, a.jobs + (size_t)(slot - a.slots) * POOL_JOBS, seq};
-        for (int c = 0; c < d.tile_mult; ++c) {
-            const long long base = ((long long)tile * d.tile_mult + c) * T;
-            if (base >= d.F) break;  // uniform: same for every thread
+        const long long t0 = (long long)tile * d.tile_v;
+        const long long t1 = min((long long)d.F, t0 + d.tile_v);
+        for (long long base = t0; base < t1; base += T) {  // uniform loop
             const long long i = base + tid;
             int rb = 0, re = 0;
-            if (i < d.F) {
+            if (i < t1) {
                 int u = ld_cg(d.log + d.front_off + i);
                 rb = __ldg(gx.row_ptr + u);
                 re = __ldg(gx.row_ptr + u + 1);
@@ -465,11 +466,24 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             desc.other_radius = sm.ql.radius[1 - x];
             desc.F = F;
             desc.front_off = (int)(front - log);
-            // about 8 tiles per CTA at most: fewer claims on the slot word
-            const int chunks = (F + T - 1) / T;
-            const int want = 8 * (int)gridDim.x;
-            desc.tile_mult = chunks > want ? (chunks + want - 1) / want : 1;
-            const int nvt = desc.dir == DIR_TD ? (chunks + desc.tile_mult - 1) / desc.tile_mult
+            // top-down tiles by work: frontiers of high average degree get
+            // tiles of fewer vertices (down to one) so that a tile reads
+            // about POOL_TILE_E entries; low-degree frontiers get tiles of T
+            // vertices, or of several chunks of T when there would be more
+            // than about 8 tiles per CTA (fewer claims on the slot word)
+            const long long m = (long long)(sm.ql.dt[x] - sm.ql.dh[x]);
+            int tv = T;
+            if (m > (long long)F * (POOL_TILE_E / T)) {
+                const long long want_v = (long long)POOL_TILE_E * F / (m > 0 ? m : 1);
+                tv = 1;
+                while (tv * 2 <= want_v) tv *= 2;
+            } else {
+                const int chunks = (F + T - 1) / T;
+                const int want = 8 * (int)gridDim.x;
+                if (chunks > want) tv = T * ((chunks + want - 1) / want);
+            }
+            desc.tile_v = tv;
+            const int nvt = desc.dir == DIR_TD ? (int)(((long long)F + tv - 1) / tv)
                                                : (nv + POOL_TILE_V - 1) / POOL_TILE_V;
             desc.nvt = nvt;
             pool_publish_and_run<T>(a, my, desc, nvt, sm);
