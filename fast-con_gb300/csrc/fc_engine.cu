@@ -23,6 +23,7 @@
 // balls, and any ball vertex adjacent to the frontier must sit on the other
 // ball's outer level.  So the meeting step may stop early and the distance is
 // still exact (the reference returns only ceil(d/2), S/make_stcon.c:1496).
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -54,11 +55,9 @@ struct StepArgs {
     TeamCounters *tc;
     int variant;
     unsigned long long *hist;  // degree-bin counters of the side (learned schedule)
+    int2 *jobs;                // row jobs (rows over TEAM_SPLIT_E entries)
+    int jcap;
 };
-
-// Engines without row splitting walk every row inside one CTA, so a
-// warp-centric step would leave a hub row to a single warp: use the hybrid.
-__host__ __device__ inline int unsplit_variant(int v) { return v == VAR_WARP ? VAR_HYBRID : v; }
 
 template <int T>
 __global__ void __launch_bounds__(T) k_step(StepArgs a)
@@ -66,8 +65,19 @@ __global__ void __launch_bounds__(T) k_step(StepArgs a)
     __shared__ SmemTopDown<T> sm;
     run_step<T>(a.mode, a.gp, a.side, a.dir, a.level, a.other_radius, a.log + a.front_begin, a.F,
                 blockIdx.x, gridDim.x, a.status, a.levels, a.log, a.cap, &a.tc->tail[a.side],
-                &a.tc->deg[a.side], &a.tc->found, &a.tc->inspected, sm, unsplit_variant(a.variant),
-                a.hist);
+                &a.tc->deg[a.side], &a.tc->found, &a.tc->inspected, sm, a.variant, a.hist,
+                TeamSink{a.jobs, a.jcap, &a.tc->njobs[0], &a.tc->nok[0]});
+}
+
+// The row jobs the preceding k_step left, on the whole grid.
+template <int T>
+__global__ void __launch_bounds__(T) k_rowjobs(StepArgs a)
+{
+    __shared__ SmemTopDown<T> sm;
+    const int nj = min(*(volatile const int *)&a.tc->nok[0], a.jcap);
+    run_team_jobs<T>(a.mode, a.gp, a.side, a.level, a.jobs, nj, blockIdx.x, gridDim.x, a.status,
+                     a.levels, a.log, a.cap, &a.tc->tail[a.side], &a.tc->deg[a.side],
+                     &a.tc->found, sm, a.hist);
 }
 
 // ---------------------------------------------------------------------------
@@ -91,6 +101,8 @@ struct PersistArgs {
     int32_t *out_hops;
     QueryStat *qstat;
     const float *mlp;  // learned schedule weights (nullable)
+    int2 *jobs;        // row jobs of top-down steps
+    int jcap;
 };
 
 template <int T>
@@ -141,11 +153,31 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
             int F;
             const int x = ql.side;
             const int32_t *front = ql_frontier(ql, a.log, nv, x, &F);
+            // row-job counters alternate by step parity: the other parity's
+            // were last read before the previous step's final barrier, so
+            // clearing them now cannot race with a reader or a pusher
+            const int par = ql.steps & 1;
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                tc->njobs[par ^ 1] = 0;
+                tc->nok[par ^ 1] = 0;
+            }
             run_step<T>(a.mode, gp, x, ql.dir, ql.radius[x], ql.radius[1 - x], front, F,
                         blockIdx.x, gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x],
-                        &tc->deg[x], &tc->found, &tc->inspected, sm, unsplit_variant(ql.variant),
-                        a.mlp ? tc->hist[x] : nullptr);
+                        &tc->deg[x], &tc->found, &tc->inspected, sm, ql.variant,
+                        a.mlp ? tc->hist[x] : nullptr,
+                        TeamSink{a.jobs, a.jcap, &tc->njobs[par], &tc->nok[par]});
             if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
+            if (ql.dir == DIR_TD) {
+                __shared__ int s_nj;
+                if (threadIdx.x == 0) s_nj = min(ld_cg(&tc->nok[par]), a.jcap);
+                __syncthreads();
+                if (s_nj > 0) {  // same value in every CTA: uniform barrier
+                    run_team_jobs<T>(a.mode, gp, x, ql.radius[x], a.jobs, s_nj, blockIdx.x,
+                                     gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x],
+                                     &tc->deg[x], &tc->found, sm, a.mlp ? tc->hist[x] : nullptr);
+                    if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
+                }
+            }
             if (threadIdx.x == 0) {
                 ql_update(ql, ld_cg(&tc->found), ld_cg(&tc->tail[x]), ld_cg_u64(&tc->deg[x]),
                           ld_cg_u64(&tc->inspected));
@@ -258,6 +290,11 @@ static int ensure_ws(DevCtx *c, size_t nv)
     FC_CUDA_TRY(cudaMalloc(&c->status, sbytes));
     FC_CUDA_TRY(cudaMalloc(&c->levels, nv * sizeof(int32_t)));
     FC_CUDA_TRY(cudaMalloc(&c->log, nv * sizeof(int32_t)));
+    if (!c->tjobs) {
+        // 2^20 jobs of 4096 entries: any step of a graph of up to 2^31 entries
+        FC_CUDA_TRY(cudaMalloc(&c->tjobs, sizeof(int2) << 20));
+        c->tjobs_cap = 1 << 20;
+    }
     FC_CUDA_TRY(cudaMemset(c->status, 0xFF, sbytes));
     FC_CUDA_TRY(cudaDeviceSynchronize());  // before any kernel on another stream reads it
     c->ws_nv = nv;
@@ -372,11 +409,22 @@ static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, in
         a.cap = nv;
         a.tc = c->tc;
         a.hist = learned ? c->tc->hist[x] : nullptr;
+        a.jobs = c->tjobs;
+        a.jcap = c->tjobs_cap;
         int grid = q.dir == DIR_TD ? (a.F + T - 1) / T : full_grid;
         if (grid > full_grid) grid = full_grid;
         if (grid < 1) grid = 1;
+        // rows over TEAM_SPLIT_E entries become row jobs for a second,
+        // full-grid launch (only possible when the frontier has that many)
+        const bool jobs = q.dir == DIR_TD && q.dt[x] - q.dh[x] > (unsigned long long)TEAM_SPLIT_E;
+        if (jobs) FC_CUDA_TRY(cudaMemsetAsync(c->tc->njobs, 0, 4 * sizeof(int), st));
+        else a.jcap = 0;
         k_step<T><<<grid, T, 0, st>>>(a);
         FC_CUDA_TRY(cudaGetLastError());
+        if (jobs) {
+            k_rowjobs<T><<<full_grid, T, 0, st>>>(a);
+            FC_CUDA_TRY(cudaGetLastError());
+        }
         FC_CUDA_TRY(cudaMemcpyAsync(c->h_tc, c->tc, sizeof(TeamCounters), cudaMemcpyDeviceToHost, st));
         FC_CUDA_TRY(cudaStreamSynchronize(st));
         ql_update(q, c->h_tc->found, c->h_tc->tail[x], c->h_tc->deg[x], c->h_tc->inspected);
@@ -524,6 +572,14 @@ static long long private_edges_default(const fc_opts &o, bool exclusive)
     return exclusive ? 4096 : 8 * 1024;
 }
 
+// Top-down tile and row-job sizes of the pool engine (entries): the options'
+// values when set, clamped to sane ranges, else the tuned defaults.
+static void pool_sizes(PoolArgs &a, const fc_opts &o)
+{
+    a.tile_e = o.tile_entries > 0 ? std::min(std::max(o.tile_entries, 1024), 1 << 22) : 16384;
+    a.split_e = o.job_entries > 0 ? std::min(std::max(o.job_entries, 1024), 1 << 22) : 4096;
+}
+
 // Device weights when the learned schedule is asked for and weights are loaded;
 // without weights the learned schedule falls back to the heuristic.
 static const float *learned_weights(DevCtx *c, const fc_opts &o)
@@ -547,6 +603,7 @@ static PoolArgs pool_args_exclusive(DevCtx *c, int mode, const fc_opts &o)
     a.log_base = c->log;
     a.log_cap = (int)c->ws_nv;
     a.private_edges = private_edges_default(o, true);
+    pool_sizes(a, o);
     a.ctr = c->b_ctr;
     a.qstat = c->qstat;
     a.mlp = learned_weights(c, o);
@@ -598,6 +655,8 @@ static int run_single(DevCtx *c, int mode, int engine, const GraphPairH &gp, int
         a.out_hops = c->d_tmp_q + 3;
         a.qstat = c->qstat;
         a.mlp = learned_weights(c, o);
+        a.jobs = c->tjobs;
+        a.jcap = c->tjobs_cap;
         rc = launch_persistent<FC_BLOCK>(c, a, stream);
         if (rc) return rc;
         rc = check_counters(c, stream);
@@ -794,6 +853,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.log_stride = c->b_log_stride;
         a.log_cap = log_cap;
         a.private_edges = private_edges_default(o, false);
+        pool_sizes(a, o);
         a.ctr = c->b_ctr;
         a.spill = c->b_spill;
         a.out_conn = d_conn;
@@ -884,6 +944,8 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.out_hops = d_hops;
         a.qstat = c->qstat;
         a.mlp = learned_weights(c, o);
+        a.jobs = c->tjobs;
+        a.jcap = c->tjobs_cap;
         rc = launch_persistent<T>(c, a, stream);
         if (rc) return rc;
         FC_CUDA_TRY(cudaEventRecord(c->evm, stream));

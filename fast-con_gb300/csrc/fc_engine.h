@@ -47,6 +47,8 @@ struct DevCtx {
     int32_t *log = nullptr;
     size_t ws_nv = 0;
     TeamCounters *tc = nullptr;      // device
+    int2 *tjobs = nullptr;           // row jobs of team steps (grid / host-loop engines)
+    int tjobs_cap = 0;
     TeamCounters *h_tc = nullptr;    // pinned mirror
     void *d_graphs = nullptr;        // GraphPair table
     size_t graphs_cap = 0;

@@ -37,9 +37,7 @@ namespace fc {
 
 constexpr int POOL_TILE_V = 8192;    // vertices per bottom-up tile
 constexpr int POOL_TILE_R = 8192;    // log entries per reset tile
-constexpr int POOL_SPLIT_E = 4096;   // row-job length
 constexpr int POOL_JOBS = 16384;     // row jobs per slot and step
-constexpr int POOL_TILE_E = 16384;   // top-down: aim for about this many entries per tile
 constexpr unsigned long long PK_MASK = (1ull << 22) - 1;
 constexpr unsigned long long POOL_IDLE_NS = 4000000000ull;  // 4 s without progress
 
@@ -65,6 +63,7 @@ struct RowJob {
 struct PoolDesc {
     int q, gidx, mode, side, dir, level, other_radius, F, front_off, nvt, cap, nreset, variant;
     int tile_v;     // top-down: frontier vertices per tile (< T, or a multiple of T)
+    int split_e;    // row-job length
     int track_hist; // count claimed vertices per degree bin (learned schedule)
     uint8_t *status;
     int32_t *levels;
@@ -91,16 +90,17 @@ struct SlotSink {
     PoolSlot *slot;
     RowJob *jobs;
     unsigned seq;
+    int split;  // job length
     __device__ bool push_row(int b, int e) const
     {
-        if (e - b <= POOL_SPLIT_E) return false;
-        int n = (e - b + POOL_SPLIT_E - 1) / POOL_SPLIT_E;
+        if (e - b <= split) return false;
+        int n = (e - b + split - 1) / split;
         int k = atomicAdd(&slot->njobs, n);
         if (k + n > POOL_JOBS) return false;  // job space exhausted: walk in place
         for (int i = 0; i < n; ++i) {
             RowJob &J = jobs[k + i];
-            J.b = b + i * POOL_SPLIT_E;
-            J.e = min(e, J.b + POOL_SPLIT_E);
+            J.b = b + i * split;
+            J.e = min(e, J.b + split);
             __threadfence();
             *(volatile unsigned *)&J.seq = seq;
         }
@@ -129,9 +129,9 @@ __device__ __forceinline__ void pool_expand(int variant, const int32_t *__restri
                                             SmemTopDown<T> &td, const SlotSink &sink)
 {
     if (variant == VAR_WARP)
-        expand_warp(col, rb, re, vis, app, sink, POOL_SPLIT_E);
+        expand_warp(col, rb, re, vis, app, sink, sink.split);
     else if (variant == VAR_THREAD)
-        expand_thread(col, rb, re, vis, app, sink, POOL_SPLIT_E);
+        expand_thread(col, rb, re, vis, app, sink, sink.split);
     else
         expand_rows<T>(col, rb, re, vis, app, td, sink);
 }
@@ -196,7 +196,7 @@ __device__ void pool_tile(const PoolArgs &a, PoolSlot *slot, int tile, unsigned 
         return;
     }
     if (d.dir == DIR_TD) {
-        SlotSink sink{slot, a.jobs + (size_t)(slot - a.slots) * POOL_JOBS, seq};
+        SlotSink sink{slot, a.jobs + (size_t)(slot - a.slots) * POOL_JOBS, seq, d.split_e};
         const long long t0 = (long long)tile * d.tile_v;
         const long long t1 = min((long long)d.F, t0 + d.tile_v);
         for (long long base = t0; base < t1; base += T) {  // uniform loop
@@ -406,6 +406,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
     desc.levels = levels;
     desc.log = log;
     desc.nreset = 0;
+    desc.split_e = a.split_e;
     // the degree histogram is counted only for the learned schedule and traces
     const bool track = (a.sched == FC_SCHED_LEARNED && a.mlp) || a.trace;
     desc.track_hist = track;
@@ -468,13 +469,13 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             desc.front_off = (int)(front - log);
             // top-down tiles by work: frontiers of high average degree get
             // tiles of fewer vertices (down to one) so that a tile reads
-            // about POOL_TILE_E entries; low-degree frontiers get tiles of T
+            // about tile_e entries; low-degree frontiers get tiles of T
             // vertices, or of several chunks of T when there would be more
             // than about 8 tiles per CTA (fewer claims on the slot word)
             const long long m = (long long)(sm.ql.dt[x] - sm.ql.dh[x]);
             int tv = T;
-            if (m > (long long)F * (POOL_TILE_E / T)) {
-                const long long want_v = (long long)POOL_TILE_E * F / (m > 0 ? m : 1);
+            if (m > (long long)F * (a.tile_e / T)) {
+                const long long want_v = (long long)a.tile_e * F / (m > 0 ? m : 1);
                 tv = 1;
                 while (tv * 2 <= want_v) tv *= 2;
             } else {

@@ -31,6 +31,8 @@ struct PoolArgs {
     size_t log_stride;
     int log_cap;
     long long private_edges;  // steps reading more entries than this are shared
+    int tile_e;               // top-down tiles aim at this many adjacency entries
+    int split_e;              // rows longer than this become row jobs of this length
     int *ctr;                 // [0] next query [1] finished [2] spill count [3] error [4] invalid
     int32_t *spill;
     int32_t *out_conn;

@@ -17,6 +17,8 @@ struct TeamCounters {
     int invalid;
     int pad;
     unsigned long long hist[2][3];  // claimed vertices per side by degree bin (learned schedule)
+    int njobs[2];                   // row-job slots taken, by step parity
+    int nok[2];                     // row jobs written (a prefix of the slots)
 };
 
 // degree bins of the frontier histogram: < 8, < 128, >= 128
@@ -343,16 +345,17 @@ __device__ __forceinline__ void topdown_variant(int variant, const DGraph &gx,
                                                 const int32_t *frontier, int F, int team_rank,
                                                 int team_size, const Vis &vis,
                                                 const AppendTarget &app, SmemTopDown<T> &sm,
-                                                const int *stop)
+                                                const int *stop, const TeamSink &sink)
 {
     if (variant == VAR_WARP)
         topdown_warps<T, VAR_WARP>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis,
-                                   app, stop);
+                                   app, stop, sink);
     else if (variant == VAR_THREAD)
         topdown_warps<T, VAR_THREAD>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis,
-                                     app, stop);
+                                     app, stop, sink);
     else
-        topdown_step<T>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis, app, sm, stop);
+        topdown_step<T>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis, app, sm, stop,
+                        sink);
 }
 
 template <int T>
@@ -361,7 +364,8 @@ __device__ void run_step(int mode, const GraphPair &gp, int side, int dir, int l
                          int team_size, uint8_t *status, int32_t *levels, int32_t *log, int cap,
                          int *tail_ctr, unsigned long long *deg_ctr, int *found,
                          unsigned long long *bu_ins, SmemTopDown<T> &sm, int variant = VAR_HYBRID,
-                         unsigned long long *hist = nullptr)
+                         unsigned long long *hist = nullptr,
+                         TeamSink sink = TeamSink{nullptr, 0, nullptr, nullptr})
 {
     const DGraph &gx = side ? gp.rev : gp.fwd;
     AppendTarget app{log, cap, side, tail_ctr, deg_ctr, gx.row_ptr, hist};
@@ -369,10 +373,11 @@ __device__ void run_step(int mode, const GraphPair &gp, int side, int dir, int l
         if (mode == MODE_BFS) {
             VisitBFS vis{levels, level + 1};
             topdown_variant<T>(variant, gx, frontier, F, team_rank, team_size, vis, app, sm,
-                               nullptr);
+                               nullptr, sink);
         } else {
             VisitSTCON vis{status, st_code(side, level + 1), side, found};
-            topdown_variant<T>(variant, gx, frontier, F, team_rank, team_size, vis, app, sm, found);
+            topdown_variant<T>(variant, gx, frontier, F, team_rank, team_size, vis, app, sm, found,
+                               sink);
         }
     } else {
         const DGraph &gr = side ? gp.fwd : gp.rev;
@@ -387,6 +392,25 @@ __device__ void run_step(int mode, const GraphPair &gp, int side, int dir, int l
     }
 }
 
+// The row jobs a top-down step left (team engines), with the step's visitor.
+template <int T>
+__device__ void run_team_jobs(int mode, const GraphPair &gp, int side, int level, const int2 *jobs,
+                              int njobs, int team_rank, int team_size, uint8_t *status,
+                              int32_t *levels, int32_t *log, int cap, int *tail_ctr,
+                              unsigned long long *deg_ctr, int *found, SmemTopDown<T> &sm,
+                              unsigned long long *hist = nullptr)
+{
+    const DGraph &gx = side ? gp.rev : gp.fwd;
+    AppendTarget app{log, cap, side, tail_ctr, deg_ctr, gx.row_ptr, hist};
+    if (mode == MODE_BFS) {
+        VisitBFS vis{levels, level + 1};
+        team_jobs<T>(gx.col, jobs, njobs, team_rank, team_size, vis, app, sm, nullptr);
+    } else {
+        VisitSTCON vis{status, st_code(side, level + 1), side, found};
+        team_jobs<T>(gx.col, jobs, njobs, team_rank, team_size, vis, app, sm, found);
+    }
+}
+
 // Root initialisation (one thread).  Writes the counters, the roots' status
 // (or level) and their log entries.
 __device__ inline void init_roots(int mode, const GraphPair &gp, int s, int t, uint8_t *status,
@@ -395,6 +419,8 @@ __device__ inline void init_roots(int mode, const GraphPair &gp, int s, int t, u
     tc->found = 0;
     tc->inspected = 0;
     tc->invalid = 0;
+    tc->njobs[0] = tc->njobs[1] = 0;
+    tc->nok[0] = tc->nok[1] = 0;
     for (int x = 0; x < 2; ++x)
         for (int b = 0; b < 3; ++b) tc->hist[x][b] = 0;
     if (mode == MODE_BFS) {

@@ -211,6 +211,32 @@ struct NoSink {
     __device__ __forceinline__ bool push_row(int, int) const { return false; }
 };
 
+// Row jobs of a team step (grid or host-loop engines): rows longer than
+// TEAM_SPLIT_E entries are cut into TEAM_SPLIT_E-entry pieces that the whole
+// team walks after the step's tiles (cap == 0: no jobs, rows walked in place).
+// Slots are taken with one atomicAdd on *njobs; a push that would pass cap
+// writes nothing and its row is walked in place, so the pushes that succeed
+// fill exactly the slots below the first failing one; *nok counts them and
+// is what the team reads.
+constexpr int TEAM_SPLIT_E = 4096;
+struct TeamSink {
+    int2 *jobs;
+    int cap;
+    int *njobs;
+    int *nok;
+    __device__ __forceinline__ bool push_row(int b, int e) const
+    {
+        if (cap == 0 || e - b <= TEAM_SPLIT_E) return false;
+        const int n = (e - b + TEAM_SPLIT_E - 1) / TEAM_SPLIT_E;
+        const int k = atomicAdd(njobs, n);
+        if (k + n > cap) return false;  // job space exhausted: walk in place
+        for (int i = 0; i < n; ++i)
+            jobs[k + i] = make_int2(b + i * TEAM_SPLIT_E, min(e, b + (i + 1) * TEAM_SPLIT_E));
+        atomicAdd(nok, n);
+        return true;
+    }
+};
+
 // ---------------------------------------------------------------------------
 // Expand one tile of frontier vertices; thread tid holds the row [rb, re) of
 // its vertex (empty when it has none).  All threads of the CTA call it.
@@ -352,10 +378,11 @@ __device__ __forceinline__ void expand_thread(const int32_t *__restrict__ col, i
 
 // Top-down step for variants 1 and 2: 32-vertex chunks dealt to the team's
 // warps; `stop_flag` is polled by each warp once per chunk.
-template <int T, int VARIANT, class Vis>
+template <int T, int VARIANT, class Vis, class Sink>
 __device__ void topdown_warps(const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
                               const int32_t *frontier, int F, int team_rank, int team_size,
-                              const Vis &vis, const AppendTarget &app, const int *stop_flag)
+                              const Vis &vis, const AppendTarget &app, const int *stop_flag,
+                              const Sink &sink)
 {
     const int lane = (int)lane_id(), wid = threadIdx.x >> 5;
     constexpr int W = T / 32;
@@ -373,9 +400,9 @@ __device__ void topdown_warps(const int32_t *__restrict__ row_ptr, const int32_t
             re = __ldg(row_ptr + u + 1);
         }
         if (VARIANT == 1)
-            expand_warp(col, rb, re, vis, app, NoSink{}, INT_MAX);
+            expand_warp(col, rb, re, vis, app, sink, TEAM_SPLIT_E);
         else
-            expand_thread(col, rb, re, vis, app, NoSink{}, INT_MAX);
+            expand_thread(col, rb, re, vis, app, sink, TEAM_SPLIT_E);
     }
 }
 
@@ -384,11 +411,11 @@ __device__ void topdown_warps(const int32_t *__restrict__ row_ptr, const int32_t
 // round-robin to the team's CTAs.  `stop_flag` (nullable) is polled once per
 // tile; a set flag ends the step early (used when the two sides have met).
 // ---------------------------------------------------------------------------
-template <int T, class Vis>
+template <int T, class Vis, class Sink>
 __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
                              const int32_t *frontier, int F, int team_rank, int team_size,
                              const Vis &vis, const AppendTarget &app, SmemTopDown<T> &sm,
-                             const int *stop_flag)
+                             const int *stop_flag, const Sink &sink)
 {
     const int tid = threadIdx.x;
     for (long long base = (long long)team_rank * T; base < F; base += (long long)team_size * T) {
@@ -399,12 +426,30 @@ __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t 
             rb = __ldg(row_ptr + u);
             re = __ldg(row_ptr + u + 1);
         }
-        expand_rows<T>(col, rb, re, vis, app, sm, NoSink{});
+        expand_rows<T>(col, rb, re, vis, app, sm, sink);
         if (stop_flag) {
             if (tid == 0) sm.stop = *(volatile const int *)stop_flag;
             __syncthreads();
             if (sm.stop) break;
         }
+    }
+}
+
+// The team walks the row jobs [0, njobs) of a step, job j on team member
+// j mod team_size; `stop_flag` (nullable) ends it early.  All threads call.
+template <int T, class Vis>
+__device__ void team_jobs(const int32_t *__restrict__ col, const int2 *jobs, int njobs,
+                          int team_rank, int team_size, const Vis &vis, const AppendTarget &app,
+                          SmemTopDown<T> &sm, const int *stop_flag)
+{
+    for (int j = team_rank; j < njobs; j += team_size) {
+        if (stop_flag) {
+            if (threadIdx.x == 0) sm.stop = *(volatile const int *)stop_flag;
+            __syncthreads();
+            if (sm.stop) break;
+        }
+        const int2 J = jobs[j];
+        walk_range(col, J.x, J.y, threadIdx.x, T, vis, app);
     }
 }
 

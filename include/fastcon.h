@@ -73,7 +73,11 @@ typedef struct fc_opts {
     int32_t variant;      /* top-down expansion variant: 0 = chosen by the
                              schedule, 1 = CTA/warp/scan hybrid, 2 = warp-
                              centric, 3 = one lane per row                  */
-    int32_t reserved[6];
+    int32_t tile_entries; /* work-sharing engine: a shared top-down tile aims
+                             at this many adjacency entries (0 = 16384)     */
+    int32_t job_entries;  /* work-sharing engine: rows longer than this are
+                             cut into jobs of this length (0 = 4096)        */
+    int32_t reserved[4];
 } fc_opts;
 
 typedef struct fc_stats {
