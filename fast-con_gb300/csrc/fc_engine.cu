@@ -573,11 +573,16 @@ static long long private_edges_default(const fc_opts &o, bool exclusive)
 }
 
 // Top-down tile and row-job sizes of the pool engine (entries): the options'
-// values when set, clamped to sane ranges, else the tuned defaults.
-static void pool_sizes(PoolArgs &a, const fc_opts &o)
+// values when set, clamped to sane ranges, else the tuned defaults.  Batches
+// (many owners, claims spread over their slots) balance best with small
+// tiles; one query on the whole grid (every claim on one slot word) with
+// large ones.
+static void pool_sizes(PoolArgs &a, const fc_opts &o, bool exclusive)
 {
-    a.tile_e = o.tile_entries > 0 ? std::min(std::max(o.tile_entries, 1024), 1 << 22) : 16384;
-    a.split_e = o.job_entries > 0 ? std::min(std::max(o.job_entries, 1024), 1 << 22) : 4096;
+    a.tile_e = o.tile_entries > 0 ? std::min(std::max(o.tile_entries, 1024), 1 << 22)
+                                  : (exclusive ? 65536 : 8192);
+    a.split_e = o.job_entries > 0 ? std::min(std::max(o.job_entries, 1024), 1 << 22)
+                                  : (exclusive ? 8192 : 2048);
 }
 
 // Device weights when the learned schedule is asked for and weights are loaded;
@@ -603,7 +608,7 @@ static PoolArgs pool_args_exclusive(DevCtx *c, int mode, const fc_opts &o)
     a.log_base = c->log;
     a.log_cap = (int)c->ws_nv;
     a.private_edges = private_edges_default(o, true);
-    pool_sizes(a, o);
+    pool_sizes(a, o, true);
     a.ctr = c->b_ctr;
     a.qstat = c->qstat;
     a.mlp = learned_weights(c, o);
@@ -690,7 +695,7 @@ int engine_bfs(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_levels, co
     if (rc) return rc;
     FC_CUDA_TRY(cudaMemsetAsync(c->levels, 0xFF, sizeof(int32_t) * (size_t)nv, stream));
     FC_CUDA_TRY(cudaEventRecord(c->ev0, stream));
-    const int engine = pick_engine(o, FC_ENGINE_BATCHED);
+    const int engine = pick_engine(o, FC_ENGINE_PERSISTENT);
     QLocal q;
     std::memset(&q, 0, sizeof(q));
     if (engine == FC_ENGINE_HOSTLOOP) {
@@ -720,7 +725,7 @@ int engine_stcon(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int32_t 
     int rc = ensure_ws(c, (size_t)nv);
     if (rc) return rc;
     FC_CUDA_TRY(cudaEventRecord(c->ev0, stream));
-    const int engine = pick_engine(o, FC_ENGINE_BATCHED);
+    const int engine = pick_engine(o, FC_ENGINE_PERSISTENT);
     QLocal q;
     std::memset(&q, 0, sizeof(q));
     if (engine == FC_ENGINE_HOSTLOOP) {
@@ -853,7 +858,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.log_stride = c->b_log_stride;
         a.log_cap = log_cap;
         a.private_edges = private_edges_default(o, false);
-        pool_sizes(a, o);
+        pool_sizes(a, o, false);
         a.ctr = c->b_ctr;
         a.spill = c->b_spill;
         a.out_conn = d_conn;
@@ -861,36 +866,46 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.qstat = c->qstat;
         a.mlp = learned_weights(c, o);
         apply_extras(a, ex);
-        // queries whose visit log outgrew their slot: one at a time, whole grid
-        PoolArgs x = pool_args_exclusive(c, MODE_STCON, o);
+        // queries whose visit log outgrew their slot: one at a time on the
+        // whole grid (grid engine over the spill list)
+        PersistArgs x;
+        std::memset(&x, 0, sizeof(x));
+        x.graphs = (const GraphPair *)c->d_graphs;
         x.graph_idx = d_gi;
         x.qs = d_s;
         x.qt = d_t;
         x.list = c->b_spill;
         x.list_count = c->b_ctr + 2;
+        x.mode = MODE_STCON;
+        x.sched = o.sched;
+        x.force_variant = forced_variant(o);
+        x.status = c->status;
+        x.levels = c->levels;
+        x.log = c->log;
+        x.tc = c->tc;
         x.out_conn = d_conn;
         x.out_hops = d_hops;
-        apply_extras(x, ex);
-        const int xgrid = c->p_grid;
+        x.qstat = c->qstat;
+        x.mlp = learned_weights(c, o);
+        x.jobs = c->tjobs;
+        x.jcap = c->tjobs_cap;
+        const int xgrid = coop_grid<T>(c);
         auto issue = [&](unsigned evflags) -> int {
             FC_CUDA_TRY(cudaMemsetAsync(c->qstat, 0, sizeof(QueryStat) * (size_t)nq, stream));
             FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 8 * sizeof(int), stream));
             int r = pool_launch(a, grid, stream);
             if (r) return r;
             FC_CUDA_TRY(cudaEventRecordWithFlags(c->evm, stream, evflags));
-            // same counter block: next and finished restart at 0, the spill
-            // count ([2]) and the error / invalid flags carry over
-            FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 2 * sizeof(int), stream));
-            return pool_launch(x, xgrid, stream);
+            return launch_persistent<T>(c, x, stream);
         };
         if (o.use_graph) {
             // the two launches and their resets as one CUDA graph, replayed
             // while every argument (pointers, sizes, grids) stays the same
-            unsigned char key[sizeof(PoolArgs) * 2 + 3 * sizeof(int)];
+            unsigned char key[sizeof(PoolArgs) + sizeof(PersistArgs) + 3 * sizeof(int)];
             std::memcpy(key, &a, sizeof(PoolArgs));
-            std::memcpy(key + sizeof(PoolArgs), &x, sizeof(PoolArgs));
+            std::memcpy(key + sizeof(PoolArgs), &x, sizeof(PersistArgs));
             int tail[3] = {grid, xgrid, nq};
-            std::memcpy(key + 2 * sizeof(PoolArgs), tail, sizeof(tail));
+            std::memcpy(key + sizeof(PoolArgs) + sizeof(PersistArgs), tail, sizeof(tail));
             static_assert(sizeof(key) <= sizeof(c->gkey), "graph key too large");
             if (!(c->gexec && c->gkey_len == sizeof(key) &&
                   std::memcmp(c->gkey, key, sizeof(key)) == 0)) {
@@ -1000,6 +1015,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
     if (sync || st) {
         rc = engine == FC_ENGINE_PERSISTENT ? check_counters(c, stream) : check_pool(c, stream, nullptr);
         if (rc) return rc;
+        if (engine == FC_ENGINE_BATCHED && (rc = check_counters(c, stream))) return rc;
     }
     if (st) {
         std::vector<QueryStat> h(nq);

@@ -415,6 +415,26 @@ def test_shared_steps_and_row_jobs(fastcon_lib, oracle_mod):
             for src in (0, 1, 50000, 7):
                 lev, _ = oracle_mod.bfs_levels(rp, col, src)
                 assert (G.bfs_levels(src, o) == lev).all(), (work_k, sch, src)
+    # small tiles and the shortest row jobs, every variant
+    for te, je in ((1024, 1024), (4096, 2048)):
+        for var in (0, 1, 2, 3):
+            o = fc.make_opts(sched=fc.SCHED_HEURISTIC, engine=fc.ENGINE_BATCHED, cta_work_k=-1,
+                             tile_entries=te, job_entries=je, variant=var)
+            conn, hops = fc.stcon_batch(G, s, t, opts=o)
+            assert (hops == want).all(), (te, je, var)
+            lev, _ = oracle_mod.bfs_levels(rp, col, 0)
+            assert (G.bfs_levels(0, o) == lev).all(), (te, je, var)
+    # hub rows (30,000 and 12,000 entries) as team row jobs of the host-loop
+    # and grid engines, in every variant and schedule
+    for eng in (fc.ENGINE_HOSTLOOP, fc.ENGINE_PERSISTENT):
+        for sch in (fc.SCHED_PLAIN, fc.SCHED_HEURISTIC):
+            for var in (0, 1, 2, 3):
+                o = fc.make_opts(sched=sch, engine=eng, variant=var)
+                for src in (0, 1, 2, 50000):
+                    lev, _ = oracle_mod.bfs_levels(rp, col, src)
+                    assert (G.bfs_levels(src, o) == lev).all(), (eng, sch, var, src)
+                conn, hops = fc.stcon_batch(G, s[:60], t[:60], opts=o)
+                assert (hops == want[:60]).all(), (eng, sch, var)
 
 
 # --------------------------------------------------------------------------
