@@ -562,14 +562,13 @@ static int check_pool(DevCtx *c, cudaStream_t st, int *invalid)
     return FC_OK;
 }
 
-static long long private_edges_default(const fc_opts &o, bool exclusive)
+static long long private_edges_default(const fc_opts &o, bool)
 {
-    // exclusive (one query at a time): share every step that has work for
-    // more than a few CTAs; batched: keep steps private up to the CTA limit;
-    // a negative setting shares every step
+    // steps reading more than 4096 entries are shared (measured best for
+    // batches between 0 and 16K); a negative setting shares every step
     if (o.cta_work_k < 0) return 0;
     if (o.cta_work_k > 0) return (long long)o.cta_work_k * 1024;
-    return exclusive ? 4096 : 8 * 1024;
+    return 4096;
 }
 
 // Top-down tile and row-job sizes of the pool engine (entries): the options'
@@ -816,9 +815,9 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
     }
     if (engine == FC_ENGINE_BATCHED) {
         if ((rc = ensure_pool(c))) return rc;
-        // two owner CTAs per SM: with tile sharing more owners do not help and
-        // each one costs a status array of the largest graph
-        int grid = pool_grid(c->sm_count, o.ctas_per_sm > 0 ? o.ctas_per_sm : 2);
+        // three owner CTAs per SM (measured best on R-MAT-24 batches against 2
+        // and 4); each owner costs a status array of the largest graph
+        int grid = pool_grid(c->sm_count, o.ctas_per_sm > 0 ? o.ctas_per_sm : 3);
         if (grid > c->p_grid) grid = c->p_grid;
         if (o.max_slots > 0 && o.max_slots < grid) grid = o.max_slots;
         // a slot's visit log bounds the queries it can finish itself; bigger

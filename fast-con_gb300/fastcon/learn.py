@@ -38,6 +38,7 @@ WEIGHTS_PATH = os.path.join(HERE, "sched_weights.json")
 N_PARAMS = 1703
 TRACE_WORDS = 24
 CANDIDATES = [(0, 0), (1, 0), (0, 1), (1, 1)]  # (side, bottom-up)
+MARGIN = float(np.log(3.0))  # logit margin a head needs to override the heuristic
 
 
 def init_weights(seed: int = 0) -> np.ndarray:
@@ -173,8 +174,11 @@ def trace_actions(tr, nq):
     return acts
 
 
-def label_states(G: Graph, s, t, tr, max_states: int, rng):
-    """Side/direction labels by scripted rollouts at sampled trace states."""
+def label_states(G: Graph, s, t, tr, max_states: int, rng, cont=SCHED_HEURISTIC):
+    """Side/direction labels by scripted rollouts at sampled trace states: at
+    each state every candidate action is forced, the trace's own actions
+    before it, schedule `cont` after it.  Returns X, Y, SW, states, C (the
+    rollout cost of each candidate) and A (the candidate the trace took)."""
     nq = len(s)
     acts = trace_actions(tr, nq)
     states = [(q, k) for q in range(nq) for k in range(len(acts[q]))]
@@ -182,7 +186,8 @@ def label_states(G: Graph, s, t, tr, max_states: int, rng):
         pick = rng.choice(len(states), size=max_states, replace=False)
         states = [states[i] for i in sorted(pick)]
     if not states:
-        return np.zeros((0, 12), np.float32), np.zeros((0, 3), np.int32), np.zeros((0, 3), np.float32), []
+        return (np.zeros((0, 12), np.float32), np.zeros((0, 3), np.int32),
+                np.zeros((0, 3), np.float32), [], np.zeros((0, 4)), np.zeros(0, np.int32))
     L = max(k for _, k in states) + 1
     rs, rt, scripts = [], [], []
     for q, k in states:
@@ -194,8 +199,7 @@ def label_states(G: Graph, s, t, tr, max_states: int, rng):
             scripts.append(sc)
             rs.append(s[q])
             rt.append(t[q])
-    hops, ins, _ = run_scripted(G, np.array(rs), np.array(rt), np.stack(scripts),
-                                sched=SCHED_HEURISTIC)
+    hops, ins, _ = run_scripted(G, np.array(rs), np.array(rt), np.stack(scripts), sched=cont)
     C = ins.reshape(len(states), len(CANDIDATES)).astype(np.float64)
     best = np.argmin(C, axis=1)  # argmin keeps the first minimum
     X = np.stack([tr["feat"][acts[q][k][3]] for q, k in states]).astype(np.float32)
@@ -213,7 +217,8 @@ def label_states(G: Graph, s, t, tr, max_states: int, rng):
     denom = np.maximum(cbest, 1.0)
     SW[:, 0] = np.clip(np.log2(1.0 + (other_side - cbest) / denom), 0.02, 8.0)
     SW[:, 1] = np.clip(np.log2(1.0 + (other_dir - cbest) / denom), 0.02, 8.0)
-    return X, Y, SW, [(q, k) for q, k in states]
+    A = np.array([CANDIDATES.index((acts[q][k][1], acts[q][k][2])) for q, k in states], np.int32)
+    return X, Y, SW, [(q, k) for q, k in states], C, A
 
 
 def label_variants(G: Graph, s, t, tr, states):
@@ -258,38 +263,70 @@ def training_graphs(total_queries=20000, scales=(18, 19, 20, 21, 22), first_seed
             yield sc, gseed, G, s, t
 
 
-def label_policy_states(G, s, t, pol, nstates, rng, log=print, tag=""):
+def label_policy_states(G, s, t, pol, nstates, rng, log=print, tag="", variants=False):
+    """Labelled states of one policy's traces.  The variant head is labelled
+    only with variants=True (timed replays); otherwise it stays unlabelled and
+    the heuristic keeps choosing the variant."""
     t0 = time.time()
     _, _, rec = run_scripted(G, s, t, None, sched=pol, trace=True)
     tr = decode(rec)
     t1 = time.time()
-    X, Y, SW, states = label_states(G, s, t, tr, nstates, rng)
+    # the learned policy's own states are continued by itself (DAgger)
+    cont = SCHED_LEARNED if pol == SCHED_LEARNED else SCHED_HEURISTIC
+    X, Y, SW, states, C, A = label_states(G, s, t, tr, nstates, rng, cont)
     t2 = time.time()
-    Y[:, 2], SW[:, 2] = label_variants(G, s, t, tr, states)
+    if variants:
+        Y[:, 2], SW[:, 2] = label_variants(G, s, t, tr, states)
+    else:
+        Y[:, 2], SW[:, 2] = -1, 0.0
     t3 = time.time()
     log(f"{tag} policy {pol}: {len(X)} states, side1 {Y[:, 0].mean():.2f} "
-        f"bu {Y[:, 1].mean():.3f} variant {np.bincount(Y[:, 2], minlength=3).tolist()} "
-        f"(trace {t1 - t0:.1f}s, rollouts {t2 - t1:.1f}s, variants {t3 - t2:.1f}s)")
-    return X, Y, SW
+        f"bu {Y[:, 1].mean():.3f} (trace {t1 - t0:.1f}s, rollouts {t2 - t1:.1f}s, "
+        f"variants {t3 - t2:.1f}s)")
+    return X, Y, SW, C, A
 
 
 def build_dataset(total_queries=20000, states_per_graph=6000, seed=0, policies=None, log=print):
     """States from the plain and heuristic traces (and from the learned
-    schedule when weights are loaded and SCHED_LEARNED is listed)."""
+    schedule when weights are loaded and SCHED_LEARNED is listed).  Returns
+    X, Y, SW and, per state, the rollout costs C, the traced action A and the
+    tracing policy P."""
     rng = np.random.default_rng(seed)
     policies = policies or (SCHED_PLAIN, SCHED_HEURISTIC)
-    Xs, Ys, Ws = [], [], []
+    parts = []
     for sc, gseed, G, s, t in training_graphs(total_queries):
         for pol in policies:
-            X, Y, SW = label_policy_states(G, s, t, pol, states_per_graph // len(policies), rng,
-                                           log, f"scale {sc} seed {gseed}")
-            Xs.append(X)
-            Ys.append(Y)
-            Ws.append(SW)
+            X, Y, SW, C, A = label_policy_states(G, s, t, pol, states_per_graph // len(policies),
+                                                 rng, log, f"scale {sc} seed {gseed}")
+            parts.append((X, Y, SW, C, A, np.full(len(X), pol, np.int32)))
         G.free()
-    X, Y, SW = np.concatenate(Xs), np.concatenate(Ys), np.concatenate(Ws)
-    perm = rng.permutation(len(X))
-    return X[perm], Y[perm], SW[perm]
+    out = [np.concatenate([p[i] for p in parts]) for i in range(6)]
+    perm = rng.permutation(len(out[0]))
+    return tuple(o[perm] for o in out)
+
+
+def policy_regret(X, C, A, P, w=None):
+    """Offline regret on states the heuristic traced: total rollout cost of
+    the chosen actions over the total of the best ones, minus 1.  w = None
+    scores the heuristic itself; otherwise the network's heads with the same
+    ln 3 margin rule as the device, falling back to the heuristic's action."""
+    m = P == SCHED_HEURISTIC
+    if not m.any():
+        return None
+    C, A, X = C[m], A[m], X[m]
+    best = C.min(axis=1)
+    act = A.copy()
+    if w is not None:
+        z = forward_np(X, w)
+        hs = np.array([CANDIDATES[a][0] for a in A])
+        hd = np.array([CANDIDATES[a][1] for a in A])
+        ds = z[:, 1] - z[:, 0]
+        side = np.where(ds > MARGIN, 1, np.where(ds < -MARGIN, 0, hs))
+        db = z[:, 3] - z[:, 2]
+        bu = np.where(db > MARGIN, 1, np.where((db < -MARGIN) | (side != hs), 0, hd))
+        act = np.array([CANDIDATES.index((int(a), int(b))) for a, b in zip(side, bu)])
+    chosen = C[np.arange(len(C)), act]
+    return float(chosen.sum() / max(best.sum(), 1.0) - 1.0)
 
 
 # ---------------------------------------------------------------------------
@@ -314,6 +351,15 @@ def evaluate(G: Graph, s, t, want_hops=None, reps=3):
     return out
 
 
+def silence_variant_head(w):
+    """Zero the variant logits: with equal logits the head never clears the
+    margin, so the heuristic keeps choosing the expansion variant."""
+    w = np.array(w, np.float32)
+    w[1472 + 4 * 32:1472 + 7 * 32] = 0.0  # W3 rows 4-6
+    w[1696 + 4:1696 + 7] = 0.0            # b3[4..6]
+    return w
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--queries", type=int, default=20000)
@@ -322,35 +368,41 @@ def main():
     ap.add_argument("--eval-queries", type=int, default=4096)
     args = ap.parse_args()
     t0 = time.time()
-    X, Y, SW = build_dataset(args.queries)
+    X, Y, SW, C, A, P = build_dataset(args.queries)
     t1 = time.time()
     nval = len(X) // 10
     w, curve = train(X[nval:], Y[nval:], epochs=args.epochs, SW=SW[nval:])
+    w = silence_variant_head(w)
     box = feature_box(X[nval:])
-    # second round: label the states the learned schedule itself visits; the
-    # validation rows of both rounds stay out of training
+    r1 = {"heuristic": policy_regret(X[:nval], C[:nval], A[:nval], P[:nval]),
+          "learned": policy_regret(X[:nval], C[:nval], A[:nval], P[:nval], w)}
+    print("round 1 validation regret", r1, flush=True)
+    # second round: label the states the learned schedule itself visits,
+    # continued by itself; the validation rows of both rounds stay out of
+    # training
     set_weights(w, box)
-    X2, Y2, SW2 = build_dataset(args.queries, states_per_graph=3000, seed=1,
-                                policies=(SCHED_LEARNED,))
+    X2, Y2, SW2, C2, A2, P2 = build_dataset(args.queries, states_per_graph=3000, seed=1,
+                                            policies=(SCHED_LEARNED,))
     nval2 = len(X2) // 10
     Xv = np.concatenate([X[:nval], X2[:nval2]])
     Yv = np.concatenate([Y[:nval], Y2[:nval2]])
     SWv = np.concatenate([SW[:nval], SW2[:nval2]])
+    Cv, Av, Pv = C[:nval], A[:nval], P[:nval]
     X = np.concatenate([X[nval:], X2[nval2:]])
     Y = np.concatenate([Y[nval:], Y2[nval2:]])
     SW = np.concatenate([SW[nval:], SW2[nval2:]])
     perm = np.random.default_rng(2).permutation(len(X))
     X, Y, SW = X[perm], Y[perm], SW[perm]
     w, curve = train(X, Y, epochs=args.epochs, SW=SW, w0=w)
+    w = silence_variant_head(w)
     box = feature_box(X)
-    nval = len(Xv)
-    X = np.concatenate([Xv, X])
-    Y = np.concatenate([Yv, Y])
-    SW = np.concatenate([SWv, SW])
-    vloss, _ = loss_grad(X[:nval], Y[:nval], w, SW[:nval])
+    ntrain = len(X)
+    vloss, _ = loss_grad(Xv, Yv, w, SWv)
     # validation accuracy per head (host forward pass in float64)
-    acc = head_accuracy(X[:nval], Y[:nval], w)
-    acc_heur = heuristic_accuracy(X[:nval], Y[:nval])
+    acc = head_accuracy(Xv, Yv, w)
+    acc_heur = heuristic_accuracy(Xv, Yv)
+    regret = {"heuristic": policy_regret(Xv[:nval], Cv, Av, Pv),
+              "learned": policy_regret(Xv[:nval], Cv, Av, Pv, w), "round1": r1}
     t2 = time.time()
     set_weights(w, box)
     ev = {}
@@ -372,13 +424,15 @@ def main():
         "box": {"lo": [float(x) for x in box[0]], "hi": [float(x) for x in box[1]]},
         "layout": "W1[32][12] b1[32] W2[32][32] b2[32] W3[7][32] b3[7]",
         "training": {"graphs": "R-MAT scale 18-22 x2, seeds 1000-1009", "queries": args.queries,
-                     "samples": int(len(X) - nval), "validation": int(nval),
+                     "samples": int(ntrain), "validation": int(len(Xv)),
                      "epochs": args.epochs, "loss_curve": [float(x) for x in curve],
                      "validation_loss": vloss, "validation_accuracy": acc,
                      "heuristic_side_accuracy": acc_heur,
-                     "rounds": "plain + heuristic traces, then the learned schedule's own states",
-                     "label_balance": {"side1": float(Y[:, 0].mean()), "bottom_up": float(Y[:, 1].mean()),
-                                       "variant": np.bincount(Y[:, 2], minlength=3).tolist()},
+                     "validation_regret": regret,
+                     "rounds": "plain + heuristic traces, then the learned schedule's own states "
+                               "continued by itself",
+                     "variant_head": "silenced (the heuristic picks the variant)",
+                     "label_balance": {"side1": float(Y[:, 0].mean()), "bottom_up": float(Y[:, 1].mean())},
                      "seconds": {"dataset": t1 - t0, "train": t2 - t1}},
         "evaluation": ev,
     }

@@ -61,22 +61,23 @@ typedef struct fc_opts {
     int32_t sched;        /* FC_SCHED_*                                     */
     int32_t engine;       /* FC_ENGINE_*                                    */
     int32_t block;        /* threads per CTA: 128, 256 or 512 (0 = tuned)   */
-    int32_t ctas_per_sm;  /* resident CTAs per SM for batched (0 = tuned)   */
+    int32_t ctas_per_sm;  /* resident CTAs per SM for batched (0 = 3)       */
     int32_t use_graph;    /* batched: capture the launch in a CUDA graph    */
     int32_t max_slots;    /* batched: cap on concurrent queries (0 = all)   */
     void   *stream;       /* cudaStream_t, NULL = the library's own stream  */
     int32_t cta_work_k;   /* work-sharing engine: a step reading more than
                              cta_work_k * 1024 adjacency entries is cut into
-                             tiles that every CTA may take (0 = 8 for
-                             batches, 4 for single queries; < 0 = share
-                             every step)                                    */
+                             tiles that every CTA may take (0 = 4;
+                             < 0 = share every step)                        */
     int32_t variant;      /* top-down expansion variant: 0 = chosen by the
                              schedule, 1 = CTA/warp/scan hybrid, 2 = warp-
                              centric, 3 = one lane per row                  */
     int32_t tile_entries; /* work-sharing engine: a shared top-down tile aims
-                             at this many adjacency entries (0 = 16384)     */
+                             at this many adjacency entries (0 = 8192 for
+                             batches, 65536 for one query on the grid)      */
     int32_t job_entries;  /* work-sharing engine: rows longer than this are
-                             cut into jobs of this length (0 = 4096)        */
+                             cut into jobs of this length (0 = 2048 for
+                             batches, 8192 for one query on the grid)       */
     int32_t reserved[4];
 } fc_opts;
 
