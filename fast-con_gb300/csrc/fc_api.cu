@@ -708,6 +708,44 @@ int fc_stcon_batch_scripted(fc_graph *g, const int32_t *d_s, const int32_t *d_t,
     return rc;
 }
 
+int fc_bfs_parents(fc_graph *g, int32_t s, int32_t *parents, int32_t *levels)
+{
+    if (validate_ptr(g, "g") || validate_ptr(parents, "parents")) return FC_ERR_INVALID;
+    if (s < 0 || s >= g->nv) {
+        set_error("source %d outside [0, %d)", s, g->nv);
+        return FC_ERR_INVALID;
+    }
+    CtxLock L;
+    if (!L.c) return L.rc;
+    return fc::engine_bfs_parents(L.c, pair_of(g), s, parents, levels, default_opts(), L.c->stream);
+}
+
+int fc_stcon_path(fc_graph *g, int32_t s, int32_t t, int32_t *path, int32_t cap, int32_t *len)
+{
+    if (validate_ptr(g, "g") || validate_ptr(len, "len") || (cap > 0 && validate_ptr(path, "path")))
+        return FC_ERR_INVALID;
+    if (cap < 0 || s < 0 || s >= g->nv || t < 0 || t >= g->nv) {
+        set_error("query (%d, %d) outside [0, %d) or cap %d < 0", s, t, g->nv, cap);
+        return FC_ERR_INVALID;
+    }
+    CtxLock L;
+    if (!L.c) return L.rc;
+    return fc::engine_stcon_path(L.c, pair_of(g), s, t, path, cap, len, default_opts(), L.c->stream);
+}
+
+int fc_validate_bfs(fc_graph *g, int32_t root, const int32_t *parents, int64_t *errors)
+{
+    if (validate_ptr(g, "g") || validate_ptr(parents, "parents") || validate_ptr(errors, "errors"))
+        return FC_ERR_INVALID;
+    if (root < 0 || root >= g->nv) {
+        set_error("root %d outside [0, %d)", root, g->nv);
+        return FC_ERR_INVALID;
+    }
+    CtxLock L;
+    if (!L.c) return L.rc;
+    return fc::engine_validate_bfs(L.c, pair_of(g), g->directed, root, parents, errors, L.c->stream);
+}
+
 int fc_selftest_wait(int32_t timeout_ms, double *elapsed_ms)
 {
     if (timeout_ms < 1 || timeout_ms > 2000) {

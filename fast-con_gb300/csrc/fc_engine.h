@@ -114,6 +114,14 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
                        int32_t *d_hops, const fc_opts &o, fc_stats *st, cudaStream_t stream,
                        bool sync, const BatchExtras *ex = nullptr);
 
+// BFS tree, shortest path, predecessor-map validation (fc_tree.cu).
+int engine_bfs_parents(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_parents,
+                       int32_t *h_levels, const fc_opts &o, cudaStream_t st);
+int engine_stcon_path(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int32_t *h_path,
+                      int32_t cap, int32_t *len, const fc_opts &o, cudaStream_t st);
+int engine_validate_bfs(DevCtx *c, const GraphPairH &gp, int directed, int32_t root,
+                        const int32_t *h_parents, int64_t *errors, cudaStream_t st);
+
 // Bounded-wait self-test: one CTA waits at a two-CTA barrier until the wait
 // expires; returns FC_ERR_TIMEOUT when it did.
 int engine_selftest_wait(DevCtx *c, int timeout_ms, double *elapsed_ms, cudaStream_t stream);

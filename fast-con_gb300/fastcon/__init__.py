@@ -39,6 +39,7 @@ EXPORTS = [
     "fc_stcon", "fc_stcon_ex", "fc_stcon_depth", "fc_stcon_batch", "fc_stcon_batch_device",
     "fc_stcon_batch_noalloc", "fc_sched_set_weights", "fc_sched_get_weights",
     "fc_mlp_loss_grad", "fc_mlp_train", "fc_stcon_batch_scripted", "fc_selftest_wait",
+    "fc_bfs_parents", "fc_stcon_path", "fc_validate_bfs",
     "fc_strerror", "fc_last_error_message", "fc_device_info", "fc_version",
 ]
 
@@ -118,6 +119,9 @@ def lib():
             "fc_stcon_batch_scripted": (ctypes.c_int, [_VP, _VP, _VP, _I32, _VP, _I32, _VP, _VP,
                                                        _VP, _VP, _I32, _VP]),
             "fc_selftest_wait": (ctypes.c_int, [_I32, _VP]),
+            "fc_bfs_parents": (ctypes.c_int, [_VP, _I32, _VP, _VP]),
+            "fc_stcon_path": (ctypes.c_int, [_VP, _I32, _I32, _VP, _I32, _VP]),
+            "fc_validate_bfs": (ctypes.c_int, [_VP, _I32, _VP, _VP]),
             "fc_strerror": (ctypes.c_char_p, [ctypes.c_int]),
             "fc_last_error_message": (ctypes.c_char_p, []),
             "fc_device_info": (ctypes.c_int, [_VP, _VP, _VP, _VP]),
@@ -255,6 +259,33 @@ class Graph:
                                       ctypes.byref(opts) if opts else None, ctypes.byref(st)),
                "fc_bfs_levels")
         return (lev, st.as_dict()) if stats else lev
+
+    def bfs_parents(self, s: int, with_levels: bool = False):
+        """Deterministic BFS tree (smallest-id parent one level closer)."""
+        par = np.empty(self.nv, np.int32)
+        lev = np.empty(self.nv, np.int32) if with_levels else None
+        _check(lib().fc_bfs_parents(self._h, int(s), _P(par), _P(lev)), "fc_bfs_parents")
+        return (par, lev) if with_levels else par
+
+    def stcon_path(self, s: int, t: int):
+        """A shortest s -> t path as a vertex array (empty if unreachable)."""
+        n = np.zeros(1, np.int32)
+        cap = 1 << 16
+        while True:
+            path = np.empty(cap, np.int32)
+            rc = lib().fc_stcon_path(self._h, int(s), int(t), _P(path), cap, _P(n))
+            if rc == ERR_OVERFLOW and n[0] > cap:
+                cap = int(n[0])
+                continue
+            _check(rc, "fc_stcon_path")
+            return path[:n[0]].copy()
+
+    def validate_bfs(self, root: int, parents):
+        """Graph500 validation counters of a predecessor map (see the header)."""
+        par = np.ascontiguousarray(parents, dtype=np.int32)
+        err = np.zeros(8, np.int64)
+        _check(lib().fc_validate_bfs(self._h, int(root), _P(par), _P(err)), "fc_validate_bfs")
+        return err
 
     def stcon(self, s: int, t: int, opts: Opts | None = None, stats: bool = False):
         c = np.zeros(1, np.int32)

@@ -256,6 +256,31 @@ int fc_stcon_batch_noalloc(const int32_t *d_row_ptr, const int32_t *d_col, int32
                            const int32_t *d_t, int32_t nq, int32_t *d_connected, int32_t *d_hops,
                            int32_t sched, void *stream);
 
+/* ---- after the traversal: trees, paths, validation -------------------------- */
+/* BFS tree from s: parents[v] = the smallest-id in-neighbour of v one level
+ * closer to s, parents[s] = s, -1 where unreachable (host array, nv).  The
+ * reference's predecessor array h_pred (S/make_stcon.c:1189-1455) holds the
+ * vertex that claimed v first; this rule makes the tree deterministic.
+ * levels (nullable, host, nv) receives the BFS levels as fc_bfs_levels. */
+int fc_bfs_parents(fc_graph *g, int32_t s, int32_t *parents, int32_t *levels);
+
+/* One shortest s -> t path: path[0] = s, ..., path[*len - 1] = t, each
+ * vertex's predecessor chosen as in fc_bfs_parents.  *len = hops + 1, or 0
+ * when t is unreachable; FC_ERR_OVERFLOW (with *len set) when cap is too
+ * small.  The reference reconstructs paths from the two colours' predecessor
+ * arrays only to validate them (validate_stcon_bfs, S/make_stcon.c:1578-1641). */
+int fc_stcon_path(fc_graph *g, int32_t s, int32_t t, int32_t *path, int32_t cap, int32_t *len);
+
+/* Validation of a predecessor map (host array, nv) on the GPU, restating the
+ * Graph500 rules of validate_bfs_result (S/reference_functions.c:99-434) for
+ * one GPU.  errors[8]: [0] the root is not its own parent, [1] a non-root
+ * vertex is its own parent or a parent is out of range, [2] no edge from a
+ * parent to its vertex, [3] a parent chain does not reach the root, [4] an
+ * edge leaves the tree, [5] an edge's endpoint depths differ by more than one
+ * (directed graphs: the head deeper than the tail + 1), [6] vertices in the
+ * tree (a count), [7] 0.  Returns FC_OK whatever the counts. */
+int fc_validate_bfs(fc_graph *g, int32_t root, const int32_t *parents, int64_t *errors);
+
 /* ---- failure detection ---------------------------------------------------- */
 /* Self-test of the bounded device-side waits every traversal kernel uses (no
  * counterpart in the reference, whose grid barrier GlobalSync,

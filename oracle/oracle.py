@@ -134,6 +134,75 @@ def count_visited_edges(row_ptr, col, levels):
                                                 _P(levels)))
 
 
+def bfs_parents(in_row_ptr, in_col, levels, s):
+    """Deterministic BFS tree from a level array: parent(v) = the smallest
+    in-neighbour one level closer to s; parent(s) = s; -1 where unreached."""
+    rp, col, lev = (np.asarray(x, np.int64) for x in (in_row_ptr, in_col, levels))
+    nv = len(rp) - 1
+    rows = np.repeat(np.arange(nv), np.diff(rp))
+    ok = (lev[rows] > 0) & (lev[col] == lev[rows] - 1)
+    par = np.full(nv, np.iinfo(np.int64).max)
+    np.minimum.at(par, rows[ok], col[ok])
+    par[par == np.iinfo(np.int64).max] = -1
+    par[lev <= 0] = -1
+    par[s] = s
+    return par.astype(np.int32)
+
+
+def validate_bfs(row_ptr, col, in_row_ptr, in_col, parents, root, directed=False):
+    """validate_bfs_result (S/reference_functions.c:99-434) restated for one
+    process with the same seven counters as fc_validate_bfs: [0] root's
+    parent wrong, [1] self parent or out of range, [2] no edge parent -> v,
+    [3] chain does not reach the root, [4] edge from the tree to outside,
+    [5] depth gap over an edge, [6] vertices in the tree."""
+    rp, cl, irp, icl = (np.asarray(x, np.int64) for x in (row_ptr, col, in_row_ptr, in_col))
+    par = np.asarray(parents, np.int64)
+    nv = len(rp) - 1
+    e = [0] * 8
+    e[0] = int(par[root] != root)
+    v = np.arange(nv)
+    bad = (v != root) & (par != -1) & ((par < 0) | (par >= nv) | (par == v))
+    e[1] = int(bad.sum())
+    e[6] = int(((par != -1) | (v == root)).sum())
+    good = (v != root) & (par >= 0) & (par < nv) & (par != v)
+    miss = 0
+    for x in np.flatnonzero(good):
+        row = icl[irp[x]:irp[x + 1]]
+        k = np.searchsorted(row, par[x])
+        miss += int(k >= len(row) or row[k] != par[x])
+    e[2] = miss
+    depth = np.full(nv, -1, np.int64)
+    depth[root] = 0
+    for x in np.flatnonzero(good | bad):
+        if depth[x] >= 0:
+            continue
+        chain, y = [], x
+        while 0 <= y < nv and depth[y] == -1 and y != root and len(chain) <= nv and par[y] != -1:
+            chain.append(y)
+            if (par[y] < 0 or par[y] >= nv or par[y] == y):
+                y = -1
+                break
+            y = par[y]
+        d = depth[y] if 0 <= y < nv and depth[y] >= 0 else None
+        if d is None:
+            for c in chain:
+                depth[c] = -2
+        else:
+            for c in reversed(chain):
+                d += 1
+                depth[c] = d
+    e[3] = int(((good | bad) & (depth < 0)).sum())
+    d = np.where(depth >= 0, depth, -1)
+    rows = np.repeat(np.arange(nv), np.diff(rp))
+    du, dv = d[rows], d[cl]
+    tree = du >= 0
+    e[4] = int((tree & (dv < 0)).sum())
+    both = tree & (dv >= 0)
+    gap = (dv - du > 1) if directed else (np.abs(dv - du) > 1)
+    e[5] = int((both & gap).sum())
+    return e
+
+
 def read_edgelist(path, relabel=False):
     """(nv, src int32, dst int32, file_directed)."""
     nv = np.zeros(1, np.int32)

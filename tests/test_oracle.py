@@ -139,3 +139,47 @@ def test_edgelist_reader_formats(oracle_mod):
         bad = _write(td, "bad.txt", "hello world\n")
         with pytest.raises(ValueError):
             oracle_mod.read_edgelist(bad)
+
+
+def _tree_case(oracle_mod):
+    rng = np.random.default_rng(41)
+    nv = 400
+    u = rng.integers(0, nv, 1500).astype(np.int32)
+    v = rng.integers(0, nv, 1500).astype(np.int32)
+    rp, col = oracle_mod.build_csr(nv, u, v)
+    lev, _ = oracle_mod.bfs_levels(rp, col, 3)
+    return rp, col, lev
+
+
+def test_parents_and_validation_restatement(oracle_mod):
+    """The tree rule (smallest-id parent one level closer) and the Graph500
+    validation counters; mistakes are planted in host arrays."""
+    rp, col, lev = _tree_case(oracle_mod)
+    par = oracle_mod.bfs_parents(rp, col, lev, 3)
+    nv = len(rp) - 1
+    reached = lev >= 0
+    assert par[3] == 3 and (par[~reached] == -1).all()
+    for x in np.flatnonzero(reached & (lev > 0)):
+        nb = col[rp[x]:rp[x + 1]]
+        assert par[x] == nb[lev[nb] == lev[x] - 1].min()
+    e = oracle_mod.validate_bfs(rp, col, rp, col, par, 3)
+    assert e[:6] == [0] * 6 and e[6] == int(reached.sum())
+    # planted mistakes, one rule each
+    bad = par.copy(); bad[3] = 7
+    assert oracle_mod.validate_bfs(rp, col, rp, col, bad, 3)[0] == 1
+    x = int(np.flatnonzero(reached & (lev > 1))[0])
+    bad = par.copy(); bad[x] = x
+    assert oracle_mod.validate_bfs(rp, col, rp, col, bad, 3)[1] == 1
+    nonnb = int(np.setdiff1d(np.flatnonzero(reached), np.append(col[rp[x]:rp[x + 1]], x))[0])
+    bad = par.copy(); bad[x] = nonnb
+    assert oracle_mod.validate_bfs(rp, col, rp, col, bad, 3)[2] >= 1
+    y = int(par[x])
+    bad = par.copy(); bad[y] = x  # a two-cycle x <-> y cut off from the root
+    e = oracle_mod.validate_bfs(rp, col, rp, col, bad, 3)
+    assert e[3] >= 2
+    unreached = np.flatnonzero(~reached)
+    if len(unreached):
+        bad = par.copy(); bad[x] = -1  # x left out of the tree: its edges leave it
+        e = oracle_mod.validate_bfs(rp, col, rp, col, bad, 3)
+        assert e[4] >= 1
+    assert nv == len(par)
