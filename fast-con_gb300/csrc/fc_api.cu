@@ -14,6 +14,7 @@
 #include "fc_engine.h"
 #include "fc_ingest.h"
 #include "fc_internal.cuh"
+#include "fc_parse.h"
 
 struct fc_graph {
     int device;
@@ -122,217 +123,6 @@ int from_device_edges(const int32_t *d_src, const int32_t *d_dst, int64_t n, int
     return FC_OK;
 }
 
-// ---------------------------------------------------------------------------
-// Edge-list files.  Formats and conventions follow the reference readers:
-//   SNAP            load_graph (S/load_graph.c:20-104): '#' comment header,
-//                   "# Nodes: N Edges: M", then "u v" per line, raw ids;
-//                   readGraphSnap (K/Util/readGraphSTD.cpp:128-145) renumbers ids
-//                   by first appearance (relabel = 1).
-//   MatrixMarket    "%%MatrixMarket ... [symmetric]", size line, 1-based pairs
-//                   (K/Util/readGraphSTD.cpp:57-75).
-//   DIMACS9         "p sp N M" and "a u v w" arcs, 1-based (K/Util/readGraphSTD.cpp:78-99).
-//   DIMACS10/METIS  "N M [fmt]" then one line of 1-based neighbours per vertex
-//                   (K/Util/readGraphSTD.cpp:101-125).
-// The vertex count is the declared one, raised to max id + 1 if an id exceeds it.
-// ---------------------------------------------------------------------------
-struct Parsed {
-    std::vector<int32_t> src, dst;
-    long long nv = 0;
-    int file_directed = -1;
-};
-
-inline bool is_digit(char c) { return c >= '0' && c <= '9'; }
-
-// parse a (possibly signed) integer at p within [p, e); returns false if none
-inline bool parse_int(const char *&p, const char *e, long long &out)
-{
-    while (p < e && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
-    if (p >= e) return false;
-    bool neg = false;
-    if (*p == '-') {
-        neg = true;
-        ++p;
-    }
-    if (p >= e || !is_digit(*p)) return false;
-    long long v = 0;
-    while (p < e && is_digit(*p)) {
-        v = v * 10 + (*p - '0');
-        if (v > (1ll << 40)) return false;
-        ++p;
-    }
-    out = neg ? -v : v;
-    return true;
-}
-
-int parse_file(const char *path, int relabel, Parsed &P)
-{
-    FILE *f = fopen(path, "rb");
-    if (!f) {
-        set_error("cannot open %s: %s", path, strerror(errno));
-        return FC_ERR_IO;
-    }
-    std::string buf;
-    if (fseek(f, 0, SEEK_END) == 0) {
-        long sz = ftell(f);
-        if (sz > 0) {
-            buf.resize((size_t)sz);
-            fseek(f, 0, SEEK_SET);
-            if (fread(&buf[0], 1, (size_t)sz, f) != (size_t)sz) {
-                fclose(f);
-                set_error("cannot read %s", path);
-                return FC_ERR_IO;
-            }
-        }
-    }
-    fclose(f);
-    const char *p = buf.data(), *end = buf.data() + buf.size();
-    int fmt = 0;  // 1 snap, 2 mm, 3 dimacs9, 4 dimacs10
-    long long declared_nodes = -1, maxid = -1;
-    bool header_done = false, mm_size = false;
-    long long d10_line = 0;
-    std::unordered_map<long long, int32_t> idmap;
-    auto map_id = [&](long long id) -> long long {
-        auto it = idmap.find(id);
-        if (it != idmap.end()) return it->second;
-        int32_t nid = (int32_t)idmap.size();
-        idmap.emplace(id, nid);
-        return nid;
-    };
-    auto push = [&](long long a, long long b) -> bool {
-        if (a < 0 || b < 0 || a > INT_MAX || b > INT_MAX) return false;
-        P.src.push_back((int32_t)a);
-        P.dst.push_back((int32_t)b);
-        if (a > maxid) maxid = a;
-        if (b > maxid) maxid = b;
-        return true;
-    };
-    while (p < end) {
-        const char *le = (const char *)memchr(p, '\n', (size_t)(end - p));
-        if (!le) le = end;
-        const char *q = p;
-        while (q < le && (*q == ' ' || *q == '\t')) ++q;
-        const char *line = q;
-        p = le + 1;
-        if (q >= le || *q == '\r') continue;
-        if (fmt == 0) {
-            if (*q == '#')
-                fmt = 1;
-            else if (le - q >= 14 && memcmp(q, "%%MatrixMarket", 14) == 0)
-                fmt = 2;
-            else if (*q == 'c' || *q == 'p')
-                fmt = 3;
-            else if (*q == '%' || is_digit(*q))
-                fmt = 4;
-            else {
-                set_error("%s: unrecognised graph format", path);
-                return FC_ERR_FORMAT;
-            }
-        }
-        std::string lstr;
-        if (fmt == 1) {
-            if (*q == '#') {
-                lstr.assign(line, le);
-                if (lstr.find("Undirected") != std::string::npos)
-                    P.file_directed = 0;
-                else if (lstr.find("Directed") != std::string::npos && P.file_directed < 0)
-                    P.file_directed = 1;
-                size_t k = lstr.find("Nodes:");
-                if (k != std::string::npos) {
-                    long long a = -1, b = -1;
-                    if (sscanf(lstr.c_str() + k, "Nodes: %lld Edges: %lld", &a, &b) >= 1)
-                        declared_nodes = a;
-                }
-                continue;
-            }
-            long long a, b;
-            if (!parse_int(q, le, a)) continue;
-            if (!parse_int(q, le, b) || a < 0 || b < 0) {
-                set_error("%s: malformed edge line", path);
-                return FC_ERR_FORMAT;
-            }
-            if (relabel) {
-                a = map_id(a);
-                b = map_id(b);
-            }
-            if (!push(a, b)) {
-                set_error("%s: vertex id out of range", path);
-                return FC_ERR_FORMAT;
-            }
-        } else if (fmt == 2) {
-            if (*q == '%') {
-                lstr.assign(line, le);
-                if (lstr.compare(0, 14, "%%MatrixMarket") == 0)
-                    P.file_directed = lstr.find("symmetric") != std::string::npos ? 0 : 1;
-                continue;
-            }
-            long long a, b, c;
-            if (!mm_size) {
-                if (!parse_int(q, le, a)) continue;
-                if (!parse_int(q, le, b) || !parse_int(q, le, c)) {
-                    set_error("%s: malformed MatrixMarket size line", path);
-                    return FC_ERR_FORMAT;
-                }
-                declared_nodes = a;
-                mm_size = true;
-                continue;
-            }
-            if (!parse_int(q, le, a)) continue;
-            if (!parse_int(q, le, b) || a < 1 || b < 1 || !push(a - 1, b - 1)) {
-                set_error("%s: malformed MatrixMarket entry", path);
-                return FC_ERR_FORMAT;
-            }
-        } else if (fmt == 3) {
-            if (*q == 'p') {
-                lstr.assign(line, le);
-                char w1[64], w2[64];
-                long long a = -1, b = -1;
-                if (sscanf(lstr.c_str(), "%63s %63s %lld %lld", w1, w2, &a, &b) == 4) declared_nodes = a;
-                continue;
-            }
-            if (*q != 'a') continue;
-            ++q;
-            long long a, b;
-            if (!parse_int(q, le, a) || !parse_int(q, le, b) || a < 1 || b < 1 || !push(a - 1, b - 1)) {
-                set_error("%s: malformed DIMACS arc", path);
-                return FC_ERR_FORMAT;
-            }
-        } else {
-            if (*q == '%') continue;
-            long long a, b, c;
-            if (!header_done) {
-                if (!parse_int(q, le, a)) continue;
-                if (!parse_int(q, le, b)) {
-                    set_error("%s: malformed METIS header", path);
-                    return FC_ERR_FORMAT;
-                }
-                declared_nodes = a;
-                P.file_directed = (parse_int(q, le, c) && c == 100) ? 1 : 0;
-                header_done = true;
-                continue;
-            }
-            if (d10_line >= declared_nodes) continue;
-            while (parse_int(q, le, a)) {
-                if (a < 1 || !push(d10_line, a - 1)) {
-                    set_error("%s: malformed METIS adjacency", path);
-                    return FC_ERR_FORMAT;
-                }
-            }
-            ++d10_line;
-        }
-    }
-    if (fmt == 0) {
-        set_error("%s: empty file", path);
-        return FC_ERR_FORMAT;
-    }
-    long long nv = (relabel && fmt == 1) ? (long long)idmap.size() : declared_nodes;
-    if (nv < maxid + 1) nv = maxid + 1;
-    if (nv > INT_MAX) {
-        set_error("%s: %lld vertices exceed the int32 limit", path, nv);
-        return FC_ERR_OVERFLOW;
-    }
-    P.nv = nv;
-    return FC_OK;
-}
 
 struct CtxLock {
     fc::DevCtx *c = nullptr;
@@ -402,12 +192,36 @@ int fc_device_info(int32_t *sm_count, int64_t *total_mem, int32_t *cc_major, int
     return FC_OK;
 }
 
+int fc_parse_edgelist(const char *path, int relabel, int nthreads, int32_t *src, int32_t *dst,
+                      int64_t cap, int64_t *n, int32_t *nv, int32_t *file_directed)
+{
+    if (validate_ptr(path, "path") || validate_ptr(n, "n") || validate_ptr(nv, "nv") ||
+        validate_ptr(file_directed, "file_directed"))
+        return FC_ERR_INVALID;
+    if (cap > 0 && (validate_ptr(src, "src") || validate_ptr(dst, "dst"))) return FC_ERR_INVALID;
+    fc::Parsed P;
+    int rc = fc::parse_edgelist_file(path, relabel, nthreads, P);
+    if (rc) return rc;
+    *n = (int64_t)P.src.size();
+    *nv = (int32_t)P.nv;
+    *file_directed = P.file_directed;
+    if (cap < *n) {
+        set_error("%lld pairs do not fit in %lld", (long long)*n, (long long)cap);
+        return FC_ERR_OVERFLOW;
+    }
+    if (*n) {
+        std::memcpy(src, P.src.data(), sizeof(int32_t) * (size_t)*n);
+        std::memcpy(dst, P.dst.data(), sizeof(int32_t) * (size_t)*n);
+    }
+    return FC_OK;
+}
+
 int fc_graph_load_edgelist(const char *path, int force_dir, int relabel, fc_graph **g)
 {
     if (validate_ptr(path, "path") || validate_ptr(g, "g")) return FC_ERR_INVALID;
     *g = nullptr;
-    Parsed P;
-    int rc = parse_file(path, relabel, P);
+    fc::Parsed P;
+    int rc = fc::parse_edgelist_file(path, relabel, 0, P);
     if (rc) return rc;
     int directed = force_dir == 0 ? 1 : force_dir == 1 ? 0 : (P.file_directed == 1 ? 1 : 0);
     return fc_graph_from_edges(P.src.data(), P.dst.data(), (int64_t)P.src.size(), (int32_t)P.nv,

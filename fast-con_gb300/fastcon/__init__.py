@@ -39,7 +39,7 @@ EXPORTS = [
     "fc_stcon", "fc_stcon_ex", "fc_stcon_depth", "fc_stcon_batch", "fc_stcon_batch_device",
     "fc_stcon_batch_noalloc", "fc_sched_set_weights", "fc_sched_get_weights",
     "fc_mlp_loss_grad", "fc_mlp_train", "fc_stcon_batch_scripted", "fc_selftest_wait",
-    "fc_bfs_parents", "fc_stcon_path", "fc_validate_bfs",
+    "fc_bfs_parents", "fc_stcon_path", "fc_validate_bfs", "fc_parse_edgelist",
     "fc_strerror", "fc_last_error_message", "fc_device_info", "fc_version",
 ]
 
@@ -120,6 +120,8 @@ def lib():
                                                        _VP, _VP, _I32, _VP]),
             "fc_selftest_wait": (ctypes.c_int, [_I32, _VP]),
             "fc_bfs_parents": (ctypes.c_int, [_VP, _I32, _VP, _VP]),
+            "fc_parse_edgelist": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _VP, _VP,
+                                                 _I64, _VP, _VP, _VP]),
             "fc_stcon_path": (ctypes.c_int, [_VP, _I32, _I32, _VP, _I32, _VP]),
             "fc_validate_bfs": (ctypes.c_int, [_VP, _I32, _VP, _VP]),
             "fc_strerror": (ctypes.c_char_p, [ctypes.c_int]),
@@ -335,6 +337,28 @@ def stcon_batch_device(graphs, s_ptr, t_ptr, nq, conn_ptr, hops_ptr, graph_idx_p
                                        ctypes.byref(st) if stats else None),
            "fc_stcon_batch_device")
     return st.as_dict() if stats else None
+
+
+def parse_edgelist(path: str, relabel: bool = False, nthreads: int = 0):
+    """Host-side parse of an edge-list file: (nv, src, dst, file_directed)."""
+    n = np.zeros(1, np.int64)
+    nv = np.zeros(1, np.int32)
+    fd = np.zeros(1, np.int32)
+    cap = 0
+    src = dst = None
+    while True:
+        rc = lib().fc_parse_edgelist(path.encode(), int(bool(relabel)), int(nthreads), _P(src),
+                                     _P(dst), cap, _P(n), _P(nv), _P(fd))
+        if rc == ERR_OVERFLOW and n[0] > cap:
+            cap = int(n[0])
+            src = np.empty(cap, np.int32)
+            dst = np.empty(cap, np.int32)
+            continue
+        _check(rc, "fc_parse_edgelist")
+        k = int(n[0])
+        if src is None:
+            src = dst = np.empty(0, np.int32)
+        return int(nv[0]), src[:k].copy(), dst[:k].copy(), int(fd[0])
 
 
 def selftest_wait(timeout_ms: int = 200):

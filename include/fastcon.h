@@ -122,6 +122,16 @@ void fc_opts_init(fc_opts *o);
  * renumbers SNAP ids by first appearance (BFS-4K), 0 keeps raw ids. */
 int fc_graph_load_edgelist(const char *path, int force_dir, int relabel, fc_graph **g);
 
+/* The host half of fc_graph_load_edgelist: parse an edge-list file with
+ * nthreads host threads (<= 0: all) into 0-based int32 pairs, in file order.
+ * Replaces the single-threaded readers load_graph (S/load_graph.c:20-104)
+ * and readSTD (K/Util/readGraphSTD.cpp).  *n = number of pairs, *nv =
+ * vertex count, *file_directed = -1 unknown, 0 undirected, 1 directed.
+ * When cap < *n nothing is copied and FC_ERR_OVERFLOW is returned with *n
+ * set (call again with larger arrays); src/dst may be NULL when cap == 0. */
+int fc_parse_edgelist(const char *path, int relabel, int nthreads, int32_t *src, int32_t *dst,
+                      int64_t cap, int64_t *n, int32_t *nv, int32_t *file_directed);
+
 /* Adopt a finished CSR from host memory (copied into 128-byte-aligned device
  * arrays).  Replaces Graph::ToCSR's output handed to
  * cudaGraph::cudaGraph(Graph&) (K/include/device/cudaGraph.cuh:14-35).
