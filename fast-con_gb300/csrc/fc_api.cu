@@ -560,6 +560,24 @@ int fc_validate_bfs(fc_graph *g, int32_t root, const int32_t *parents, int64_t *
     return fc::engine_validate_bfs(L.c, pair_of(g), g->directed, root, parents, errors, L.c->stream);
 }
 
+int fc_stcon_multiseed(fc_graph *g, int32_t s, int32_t t, int32_t nseeds, uint64_t seed,
+                       int32_t *connected, fc_stats *stats)
+{
+    if (validate_ptr(g, "g") || validate_ptr(connected, "connected")) return FC_ERR_INVALID;
+    if (s < 0 || s >= g->nv || t < 0 || t >= g->nv) {
+        set_error("query (%d, %d) outside [0, %d)", s, t, g->nv);
+        return FC_ERR_INVALID;
+    }
+    if (g->directed) {
+        set_error("multi-seed connectivity needs an undirected graph");
+        return FC_ERR_UNSUPPORTED;
+    }
+    CtxLock L;
+    if (!L.c) return L.rc;
+    return fc::engine_stcon_multiseed(L.c, pair_of(g), s, t, nseeds, seed, connected, stats,
+                                      L.c->stream);
+}
+
 int fc_selftest_wait(int32_t timeout_ms, double *elapsed_ms)
 {
     if (timeout_ms < 1 || timeout_ms > 2000) {

@@ -301,6 +301,8 @@ static int ensure_ws(DevCtx *c, size_t nv)
     return FC_OK;
 }
 
+int ensure_workspace(DevCtx *c, size_t nv) { return ensure_ws(c, nv); }
+
 static int ensure_graphs(DevCtx *c, const GraphPairH *gps, int n, cudaStream_t st)
 {
     if ((size_t)n > c->graphs_cap) {

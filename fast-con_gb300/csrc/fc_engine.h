@@ -122,6 +122,14 @@ int engine_stcon_path(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int
 int engine_validate_bfs(DevCtx *c, const GraphPairH &gp, int directed, int32_t root,
                         const int32_t *h_parents, int64_t *errors, cudaStream_t st);
 
+// s~t connectivity by multi-seed region growth (fc_multiseed.cu)
+int engine_stcon_multiseed(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int32_t nseeds,
+                           unsigned long long seed, int32_t *connected, fc_stats *st,
+                           cudaStream_t stream);
+
+// Grow the single-query workspaces (status, levels, log, team jobs) to nv.
+int ensure_workspace(DevCtx *c, size_t nv);
+
 // Bounded-wait self-test: one CTA waits at a two-CTA barrier until the wait
 // expires; returns FC_ERR_TIMEOUT when it did.
 int engine_selftest_wait(DevCtx *c, int timeout_ms, double *elapsed_ms, cudaStream_t stream);

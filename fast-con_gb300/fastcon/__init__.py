@@ -40,6 +40,7 @@ EXPORTS = [
     "fc_stcon_batch_noalloc", "fc_sched_set_weights", "fc_sched_get_weights",
     "fc_mlp_loss_grad", "fc_mlp_train", "fc_stcon_batch_scripted", "fc_selftest_wait",
     "fc_bfs_parents", "fc_stcon_path", "fc_validate_bfs", "fc_parse_edgelist",
+    "fc_stcon_multiseed",
     "fc_strerror", "fc_last_error_message", "fc_device_info", "fc_version",
 ]
 
@@ -120,6 +121,7 @@ def lib():
                                                        _VP, _VP, _I32, _VP]),
             "fc_selftest_wait": (ctypes.c_int, [_I32, _VP]),
             "fc_bfs_parents": (ctypes.c_int, [_VP, _I32, _VP, _VP]),
+            "fc_stcon_multiseed": (ctypes.c_int, [_VP, _I32, _I32, _I32, ctypes.c_uint64, _VP, _VP]),
             "fc_parse_edgelist": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _VP, _VP,
                                                  _I64, _VP, _VP, _VP]),
             "fc_stcon_path": (ctypes.c_int, [_VP, _I32, _I32, _VP, _I32, _VP]),
@@ -261,6 +263,15 @@ class Graph:
                                       ctypes.byref(opts) if opts else None, ctypes.byref(st)),
                "fc_bfs_levels")
         return (lev, st.as_dict()) if stats else lev
+
+    def stcon_multiseed(self, s: int, t: int, nseeds: int = 320, seed: int = 1,
+                        stats: bool = False):
+        """Connectivity only, by multi-seed region growth (undirected)."""
+        c = np.zeros(1, np.int32)
+        st = Stats()
+        _check(lib().fc_stcon_multiseed(self._h, int(s), int(t), int(nseeds), int(seed), _P(c),
+                                        ctypes.byref(st)), "fc_stcon_multiseed")
+        return (bool(c[0]), st.as_dict()) if stats else bool(c[0])
 
     def bfs_parents(self, s: int, with_levels: bool = False):
         """Deterministic BFS tree (smallest-id parent one level closer)."""

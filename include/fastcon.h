@@ -291,6 +291,17 @@ int fc_stcon_path(fc_graph *g, int32_t s, int32_t t, int32_t *path, int32_t cap,
  * tree (a count), [7] 0.  Returns FC_OK whatever the counts. */
 int fc_validate_bfs(fc_graph *g, int32_t root, const int32_t *parents, int64_t *errors);
 
+/* Is t reachable from s (undirected graphs), by growing BFS regions from
+ * nseeds seeds at once -- s, t and nseeds - 2 vertices drawn by a hash of
+ * `seed` -- and joining regions in a device union-find whenever an edge
+ * links two of them (the BFS_4K_MULTI fork, KM/src/device/
+ * BFS_WorkEfficient.cu:9-233 with the closure of BFS_WE_AdjMatrixAnalysis.cu:
+ * 4-35).  Exact: yes as soon as s's and t's regions are joined, no when the
+ * growth stops first.  No distance.  2 <= nseeds <= 4096; directed graphs:
+ * FC_ERR_UNSUPPORTED.  stats (nullable): steps = levels grown. */
+int fc_stcon_multiseed(fc_graph *g, int32_t s, int32_t t, int32_t nseeds, uint64_t seed,
+                       int32_t *connected, fc_stats *stats);
+
 /* ---- failure detection ---------------------------------------------------- */
 /* Self-test of the bounded device-side waits every traversal kernel uses (no
  * counterpart in the reference, whose grid barrier GlobalSync,
