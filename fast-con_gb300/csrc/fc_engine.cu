@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
         while (true) {
             if (threadIdx.x == 0 && !ql.done) {
                 ql_decide(ql, a.sched, 1, bu_cap, 0, a.force_variant);
-                if (a.mlp) {  // every CTA computes the same decision
+                if (a.mlp && mlp_worth(ql)) {  // every CTA computes the same decision
                     float f[MLP_IN], o[MLP_OUT];
                     ql_features(ql, f);
                     if (mlp_in_box(a.mlp, f)) {
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
             run_step<T>(a.mode, gp, x, ql.dir, ql.radius[x], ql.radius[1 - x], front, F,
                         blockIdx.x, gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x],
                         &tc->deg[x], &tc->found, &tc->inspected, sm, ql.variant,
-                        a.mlp ? tc->hist[x] : nullptr,
+                        a.mlp ? &tc->hist[x] : nullptr,
                         TeamSink{a.jobs, a.jcap, &tc->njobs[par], &tc->nok[par]});
             if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
             if (ql.dir == DIR_TD) {
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
                 if (s_nj > 0) {  // same value in every CTA: uniform barrier
                     run_team_jobs<T>(a.mode, gp, x, ql.radius[x], a.jobs, s_nj, blockIdx.x,
                                      gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x],
-                                     &tc->deg[x], &tc->found, sm, a.mlp ? tc->hist[x] : nullptr);
+                                     &tc->deg[x], &tc->found, sm, a.mlp ? &tc->hist[x] : nullptr);
                     if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
                 }
             }
@@ -182,9 +182,7 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
                 ql_update(ql, ld_cg(&tc->found), ld_cg(&tc->tail[x]), ld_cg_u64(&tc->deg[x]),
                           ld_cg_u64(&tc->inspected));
                 if (a.mlp) {
-                    unsigned long long h3[3];
-                    for (int b = 0; b < 3; ++b) h3[b] = ld_cg_u64(&tc->hist[x][b]);
-                    ql_update_hist(ql, x, h3);
+                    ql_update_hist(ql, x, ld_cg_u64(&tc->hist[x]));
                 }
             }
             __syncthreads();
@@ -385,7 +383,7 @@ static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, in
     const bool learned = sched == FC_SCHED_LEARNED && c->mlp_ready;
     while (!q.done) {
         ql_decide(q, sched, 1, bu_cap, 0, force_variant);
-        if (learned) {
+        if (learned && mlp_worth(q)) {
             float f[MLP_IN], o[MLP_OUT];
             ql_features(q, f);
             if (mlp_in_box(c->h_mlp, f)) {
@@ -410,7 +408,7 @@ static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, in
         a.log = c->log;
         a.cap = nv;
         a.tc = c->tc;
-        a.hist = learned ? c->tc->hist[x] : nullptr;
+        a.hist = learned ? &c->tc->hist[x] : nullptr;
         a.jobs = c->tjobs;
         a.jcap = c->tjobs_cap;
         int grid = q.dir == DIR_TD ? (a.F + T - 1) / T : full_grid;

@@ -162,7 +162,7 @@ __device__ void pool_tile(const PoolArgs &a, PoolSlot *slot, int tile, unsigned 
     const GraphPair &gp = a.graphs[d.gidx];
     const DGraph &gx = d.side ? gp.rev : gp.fwd;
     AppendTarget app{d.log, d.cap, d.side, &slot->tc.tail[d.side], &slot->tc.deg[d.side],
-                     gx.row_ptr, d.track_hist ? slot->tc.hist[d.side] : nullptr};
+                     gx.row_ptr, d.track_hist ? &slot->tc.hist[d.side] : nullptr};
     if (tile >= d.nvt) {
         // row job: wait (bounded) until its descriptor carries this step's seq
         RowJob *J = a.jobs + (size_t)(slot - a.slots) * POOL_JOBS + (tile - d.nvt);
@@ -416,10 +416,11 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             // warp 0 decides: policy, then the MLP (warp-level), then a script
             if (tid == 0) ql_decide(sm.ql, a.sched, 1, bu_cap, 1, a.force_variant);
             __syncwarp();
-            if (track) {
+            const bool consult = a.sched == FC_SCHED_LEARNED && a.mlp && mlp_worth(sm.ql);
+            if (a.trace || consult) {
                 float f[MLP_IN];
                 ql_features(sm.ql, f);
-                if (a.sched == FC_SCHED_LEARNED && a.mlp && mlp_in_box(a.mlp, f)) {
+                if (consult && mlp_in_box(a.mlp, f)) {
                     float o[MLP_OUT];
                     mlp_forward_warp(a.mlp, f, o);
                     if (tid == 0) {
@@ -457,7 +458,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
         if (!sm.publish) {
             run_step<T>(a.mode, gp, x, DIR_TD, sm.ql.radius[x], sm.ql.radius[1 - x], front, F, 0, 1,
                         status, levels, log, cap, &my->tc.tail[x], &my->tc.deg[x], &my->tc.found,
-                        &my->tc.inspected, sm.td, sm.ql.variant, track ? my->tc.hist[x] : nullptr);
+                        &my->tc.inspected, sm.td, sm.ql.variant, track ? &my->tc.hist[x] : nullptr);
             __syncthreads();
         } else {
             desc.side = x;
@@ -497,9 +498,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             ql_update(sm.ql, ld_cg(&my->tc.found), ld_cg(&my->tc.tail[x]), ld_cg_u64(&my->tc.deg[x]),
                       ld_cg_u64(&my->tc.inspected));
             if (track) {
-                unsigned long long h3[3];
-                for (int b = 0; b < 3; ++b) h3[b] = ld_cg_u64(&my->tc.hist[x][b]);
-                ql_update_hist(sm.ql, x, h3);
+                ql_update_hist(sm.ql, x, ld_cg_u64(&my->tc.hist[x]));
             }
             if (a.trace) {
                 const int k = atomicAdd(a.trace_count, 1);

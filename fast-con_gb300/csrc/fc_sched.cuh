@@ -16,13 +16,19 @@ struct TeamCounters {
     int bar[2];
     int invalid;
     int pad;
-    unsigned long long hist[2][3];  // claimed vertices per side by degree bin (learned schedule)
+    unsigned long long hist[2];     // claimed vertices per side of degree < 8 (low 32 bits)
+                                    // and >= 128 (high 32 bits), learned schedule
     int njobs[2];                   // row-job slots taken, by step parity
     int nok[2];                     // row jobs written (a prefix of the slots)
 };
 
-// degree bins of the frontier histogram: < 8, < 128, >= 128
+// degree bins of the frontier histogram: < 8, < 128, >= 128; the counters
+// keep the outer two packed in one word (the middle one is the remainder)
 __host__ __device__ inline int deg_bin(long long d) { return d < 8 ? 0 : (d < 128 ? 1 : 2); }
+__host__ __device__ inline unsigned long long hist_word(long long d)
+{
+    return d < 8 ? 1ull : (d >= 128 ? (1ull << 32) : 0ull);
+}
 
 struct GraphPair {
     DGraph fwd, rev;
@@ -48,7 +54,7 @@ struct QLocal {
     int two;
     int nv;
     long long ne;
-    unsigned long long hh[2][3], ht[2][3];  // histogram counters at head / tail
+    unsigned long long hh[2][2], ht[2][2];  // bins < 8 and >= 128 at head / tail
     int last_side;
     float feat[12];                          // features of the last decision
 };
@@ -57,9 +63,13 @@ __host__ __device__ inline void ql_start(QLocal &q, int two, int nv, long long n
                                          unsigned long long deg_s, unsigned long long deg_t)
 {
     for (int x = 0; x < 2; ++x)
-        for (int b = 0; b < 3; ++b) q.hh[x][b] = q.ht[x][b] = 0;
-    q.ht[0][deg_bin((long long)deg_s)] = 1;
-    if (two && s != t) q.ht[1][deg_bin((long long)deg_t)] = 1;
+        for (int b = 0; b < 2; ++b) q.hh[x][b] = q.ht[x][b] = 0;
+    q.ht[0][0] = deg_s < 8;
+    q.ht[0][1] = deg_s >= 128;
+    if (two && s != t) {
+        q.ht[1][0] = deg_t < 8;
+        q.ht[1][1] = deg_t >= 128;
+    }
     q.last_side = -1;
     q.head[0] = q.head[1] = 0;
     q.tail[0] = 1;
@@ -174,13 +184,14 @@ __host__ __device__ inline void ql_update(QLocal &q, int found, int tail_x,
     }
 }
 
-// After ql_update for side x: move the side's histogram window forward.
-__host__ __device__ inline void ql_update_hist(QLocal &q, int x, const unsigned long long *h3)
+// After ql_update for side x: move the side's histogram window forward
+// (`word` = the side's packed counter).
+__host__ __device__ inline void ql_update_hist(QLocal &q, int x, unsigned long long word)
 {
-    for (int b = 0; b < 3; ++b) {
-        q.hh[x][b] = q.ht[x][b];
-        q.ht[x][b] = h3[b];
-    }
+    q.hh[x][0] = q.ht[x][0];
+    q.hh[x][1] = q.ht[x][1];
+    q.ht[x][0] = word & 0xFFFFFFFFull;
+    q.ht[x][1] = word >> 32;
 }
 
 // ---------------------------------------------------------------------------
@@ -205,6 +216,15 @@ constexpr int MLP_W1 = 0, MLP_B1 = MLP_W1 + MLP_H * MLP_IN, MLP_W2 = MLP_B1 + ML
               MLP_B2 = MLP_W2 + MLP_H * MLP_H, MLP_W3 = MLP_B2 + MLP_H,
               MLP_B3 = MLP_W3 + MLP_OUT * MLP_H, MLP_PARAMS = MLP_B3 + MLP_OUT;
 constexpr int MLP_BOX = MLP_PARAMS, MLP_STORE = MLP_PARAMS + 2 * MLP_IN;
+// The network is consulted only when the heuristic's step would read at
+// least this many adjacency entries: smaller steps cost little whichever way
+// they go, and skipping them keeps the inference off the short-step path.
+constexpr long long MLP_MIN_EDGES = 1024;
+
+__host__ __device__ inline bool mlp_worth(const QLocal &q)
+{
+    return (long long)(q.dt[q.side] - q.dh[q.side]) >= MLP_MIN_EDGES;
+}
 static_assert(MLP_PARAMS == 1703, "parameter count");
 
 __host__ __device__ inline void ql_features(const QLocal &q, float *f)
@@ -223,13 +243,10 @@ __host__ __device__ inline void ql_features(const QLocal &q, float *f)
     f[4] = q.ne > 0 ? (float)un / (float)q.ne : 0.f;
     f[5] = q.last_side < 0 ? 0.5f : (float)q.last_side;
     for (int x = 0; x < 2; ++x) {
-        float h[3], tot = 0.f;
-        for (int b = 0; b < 3; ++b) {
-            h[b] = (float)(q.ht[x][b] - q.hh[x][b]);
-            tot += h[b];
-        }
-        f[6 + 2 * x] = tot > 0.f ? h[0] / tot : 0.f;
-        f[7 + 2 * x] = tot > 0.f ? h[2] / tot : 0.f;
+        // every claim is counted, so the bins of the frontier add up to its size
+        const float tot = (float)(q.tail[x] - q.head[x]);
+        f[6 + 2 * x] = tot > 0.f ? (float)(q.ht[x][0] - q.hh[x][0]) / tot : 0.f;
+        f[7 + 2 * x] = tot > 0.f ? (float)(q.ht[x][1] - q.hh[x][1]) / tot : 0.f;
         f[10 + x] = log2f(1.f + (float)q.radius[x]) * 0.125f;
     }
 }
@@ -422,7 +439,7 @@ __device__ inline void init_roots(int mode, const GraphPair &gp, int s, int t, u
     tc->njobs[0] = tc->njobs[1] = 0;
     tc->nok[0] = tc->nok[1] = 0;
     for (int x = 0; x < 2; ++x)
-        for (int b = 0; b < 3; ++b) tc->hist[x][b] = 0;
+        tc->hist[x] = 0;
     if (mode == MODE_BFS) {
         levels[s] = 0;
         log[0] = s;
@@ -430,11 +447,11 @@ __device__ inline void init_roots(int mode, const GraphPair &gp, int s, int t, u
         tc->tail[1] = 0;
         tc->deg[0] = (unsigned long long)(gp.fwd.row_ptr[s + 1] - gp.fwd.row_ptr[s]);
         tc->deg[1] = 0;
-        tc->hist[0][deg_bin((long long)tc->deg[0])] = 1;
+        tc->hist[0] = hist_word((long long)tc->deg[0]);
         return;
     }
-    tc->hist[0][deg_bin((long long)(gp.fwd.row_ptr[s + 1] - gp.fwd.row_ptr[s]))] = 1;
-    if (s != t) tc->hist[1][deg_bin((long long)(gp.rev.row_ptr[t + 1] - gp.rev.row_ptr[t]))] = 1;
+    tc->hist[0] = hist_word((long long)(gp.fwd.row_ptr[s + 1] - gp.fwd.row_ptr[s]));
+    if (s != t) tc->hist[1] = hist_word((long long)(gp.rev.row_ptr[t + 1] - gp.rev.row_ptr[t]));
     status[s] = st_code(0, 0);
     log[0] = s;
     tc->tail[0] = 1;

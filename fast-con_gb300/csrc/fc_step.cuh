@@ -33,7 +33,8 @@ struct AppendTarget {
     int *tail;          // cumulative append counter of this side
     unsigned long long *deg;  // cumulative degree sum of appended vertices
     const int32_t *row_ptr;   // CSR used to expand this side next time
-    unsigned long long *hist; // nullable: claimed vertices per degree bin (<8, <128, >=128)
+    unsigned long long *hist; // nullable: packed counts of claimed vertices of degree < 8
+                              // (low 32 bits) and >= 128 (high 32 bits)
 };
 
 __device__ __forceinline__ void log_write(const AppendTarget &a, int pos, int v)
@@ -56,7 +57,7 @@ __device__ __forceinline__ void warp_append(const int (&c)[K], const AppendTarge
     int incl = warp_inclusive_scan(cnt);
     int total = __shfl_sync(0xffffffffu, incl, 31);
     long long dsum = 0;
-    int h0 = 0, h1 = 0, h2 = 0;
+    int h0 = 0, h2 = 0;
 #pragma unroll
     for (int k = 0; k < K; ++k)
         if (c[k] >= 0) {
@@ -72,15 +73,9 @@ __device__ __forceinline__ void warp_append(const int (&c)[K], const AppendTarge
         atomicAdd(a.deg, (unsigned long long)dsum);
     }
     if (a.hist) {  // uniform: same pointer in every lane
-        h1 = cnt - h0 - h2;
-        h0 = warp_sum_i(h0);
-        h1 = warp_sum_i(h1);
-        h2 = warp_sum_i(h2);
-        if (lane_id() == 0) {
-            if (h0) atomicAdd(a.hist + 0, (unsigned long long)h0);
-            if (h1) atomicAdd(a.hist + 1, (unsigned long long)h1);
-            if (h2) atomicAdd(a.hist + 2, (unsigned long long)h2);
-        }
+        const unsigned long long w =
+            (unsigned long long)warp_sum_i(h0) | ((unsigned long long)warp_sum_i(h2) << 32);
+        if (lane_id() == 0 && w) atomicAdd(a.hist, w);
     }
     base = __shfl_sync(0xffffffffu, base, 0);
     int pos = base + incl - cnt;

@@ -191,24 +191,28 @@ def test_box_gate_and_margin(fastcon_lib, oracle_mod):
         assert (hops == want).all()
         d = learn.decode(rec)
         order = np.lexsort((d["step"], d["q"]))
-        return d["q"][order], d["step"][order], d["side"][order], d["dir"][order]
+        return (d["q"][order], d["step"][order], d["side"][order], d["dir"][order],
+                d["cost"][order])
 
     heur = trace(fc.SCHED_HEURISTIC)
     w = np.zeros(1703, np.float32)
     w[1696 + 1] = 10.0  # side-1 logit: always expand t's side, with a clear margin
     full = (np.full(12, -1e9), np.full(12, 1e9))
     learn.set_weights(w, full)
-    q, step, side, _ = trace(fc.SCHED_LEARNED)
+    q, step, side, _, cost = trace(fc.SCHED_LEARNED)
     two = s[q] != t[q]
-    assert two.any() and (side[two] == 1).all()
+    # the network decides every step the heuristic would make read >= 1024
+    # entries; a side-0 step is one the heuristic chose as a short step
+    assert two.any() and (side[two] == 1).mean() > 0.5
+    assert (cost[two & (side == 0)] < 1024).all()
     # an empty box: the heuristic decides every step
     learn.set_weights(w, (np.ones(12), np.zeros(12)))
     got = trace(fc.SCHED_LEARNED)
-    for a, b in zip(got, heur):
+    for a, b in zip(got[:4], heur[:4]):
         assert (a == b).all()
     # a margin below ln 3: the heuristic decides as well
     w[1696 + 1] = 0.5
     learn.set_weights(w, full)
     got = trace(fc.SCHED_LEARNED)
-    for a, b in zip(got, heur):
+    for a, b in zip(got[:4], heur[:4]):
         assert (a == b).all()
