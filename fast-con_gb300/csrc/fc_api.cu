@@ -487,6 +487,71 @@ int fc_stcon_batch_device(fc_graph *const *gs, int32_t ngraphs, const int32_t *d
                                   d_hops, o, stats, pick_stream(opts, L.c), stats != nullptr);
 }
 
+// Autotuner: every candidate runs the caller's sample batch `reps` times
+// after one warm-up run; the median kernel time picks the winner.  The
+// candidates are the knobs the batched engine measured sensitive to on
+// R-MAT and grid workloads: resident owner CTAs per SM, the private-step
+// threshold and the shared tile size.
+int fc_autotune_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *d_graph_idx,
+                      const int32_t *d_s, const int32_t *d_t, int32_t nq, int32_t reps,
+                      fc_opts *inout, double *best_ms)
+{
+    if (validate_ptr(gs, "gs") || validate_ptr(d_s, "s") || validate_ptr(d_t, "t") ||
+        validate_ptr(inout, "opts"))
+        return FC_ERR_INVALID;
+    if (nq <= 0 || ngraphs < 1 || reps < 1 || reps > 100) {
+        set_error("autotune: nq %d, ngraphs %d, reps %d", nq, ngraphs, reps);
+        return FC_ERR_INVALID;
+    }
+    std::vector<fc::GraphPairH> pairs((size_t)ngraphs);
+    for (int i = 0; i < ngraphs; ++i) {
+        if (!gs[i]) return FC_ERR_INVALID;
+        pairs[(size_t)i] = pair_of(gs[i]);
+    }
+    CtxLock L;
+    if (!L.c) return L.rc;
+    cudaStream_t st = pick_stream(inout, L.c);
+    int32_t *dc = nullptr;
+    FC_CUDA_TRY(cudaMallocAsync(&dc, sizeof(int32_t) * 2 * (size_t)nq, st));
+    const int ctas[] = {2, 3, 4};
+    const int workk[] = {2, 4, 8};
+    const int tiles[] = {4096, 8192, 16384};
+    fc_opts best = *inout;
+    double best_t = -1;
+    int rc = FC_OK;
+    for (int a : ctas)
+        for (int w : workk)
+            for (int te : tiles) {
+                fc_opts o = *inout;
+                o.engine = FC_ENGINE_BATCHED;
+                o.use_graph = 0;
+                o.ctas_per_sm = a;
+                o.cta_work_k = w;
+                o.tile_entries = te;
+                std::vector<double> ts;
+                for (int r = 0; r <= reps && rc == FC_OK; ++r) {
+                    fc_stats s;
+                    rc = fc::engine_stcon_batch(L.c, pairs.data(), ngraphs, d_graph_idx, d_s, d_t,
+                                                nq, dc, dc + nq, o, &s, st, true);
+                    if (r) ts.push_back(s.kernel_ms[0] + s.kernel_ms[1]);
+                }
+                if (rc) break;
+                std::sort(ts.begin(), ts.end());
+                const double med = ts[ts.size() / 2];
+                if (best_t < 0 || med < best_t) {
+                    best_t = med;
+                    best = o;
+                }
+            }
+    cudaFreeAsync(dc, st);
+    cudaStreamSynchronize(st);
+    if (rc) return rc;
+    best.use_graph = inout->use_graph;
+    *inout = best;
+    if (best_ms) *best_ms = best_t;
+    return FC_OK;
+}
+
 int fc_stcon_batch_scripted(fc_graph *g, const int32_t *d_s, const int32_t *d_t, int32_t nq,
                             const uint8_t *d_script, int32_t script_len, const fc_opts *opts,
                             int32_t *d_hops, int64_t *d_inspected, int32_t *d_trace,

@@ -40,7 +40,7 @@ EXPORTS = [
     "fc_stcon_batch_noalloc", "fc_sched_set_weights", "fc_sched_get_weights",
     "fc_mlp_loss_grad", "fc_mlp_train", "fc_stcon_batch_scripted", "fc_selftest_wait",
     "fc_bfs_parents", "fc_stcon_path", "fc_validate_bfs", "fc_parse_edgelist",
-    "fc_stcon_multiseed",
+    "fc_stcon_multiseed", "fc_autotune_batch",
     "fc_strerror", "fc_last_error_message", "fc_device_info", "fc_version",
 ]
 
@@ -122,6 +122,7 @@ def lib():
             "fc_selftest_wait": (ctypes.c_int, [_I32, _VP]),
             "fc_bfs_parents": (ctypes.c_int, [_VP, _I32, _VP, _VP]),
             "fc_stcon_multiseed": (ctypes.c_int, [_VP, _I32, _I32, _I32, ctypes.c_uint64, _VP, _VP]),
+            "fc_autotune_batch": (ctypes.c_int, [_VP, _I32, _VP, _VP, _VP, _I32, _I32, _VP, _VP]),
             "fc_parse_edgelist": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _VP, _VP,
                                                  _I64, _VP, _VP, _VP]),
             "fc_stcon_path": (ctypes.c_int, [_VP, _I32, _I32, _VP, _I32, _VP]),
@@ -348,6 +349,26 @@ def stcon_batch_device(graphs, s_ptr, t_ptr, nq, conn_ptr, hops_ptr, graph_idx_p
                                        ctypes.byref(st) if stats else None),
            "fc_stcon_batch_device")
     return st.as_dict() if stats else None
+
+
+def autotune_batch(graphs, s_ptr, t_ptr, nq, graph_idx_ptr=None, opts: Opts | None = None,
+                   reps: int = 3):
+    """Pick the fastest batched-engine settings on a sample batch (device
+    pointers).  Returns (opts, best_ms)."""
+    if isinstance(graphs, Graph):
+        graphs = [graphs]
+    arr = (ctypes.c_void_p * len(graphs))(*[g.handle.value for g in graphs])
+    o = Opts()
+    if opts is not None:
+        ctypes.memmove(ctypes.byref(o), ctypes.byref(opts), ctypes.sizeof(Opts))
+    else:
+        lib().fc_opts_init(ctypes.byref(o))
+    ms = np.zeros(1, np.float64)
+    _check(lib().fc_autotune_batch(arr, len(graphs),
+                                   ctypes.c_void_p(graph_idx_ptr) if graph_idx_ptr else None,
+                                   ctypes.c_void_p(s_ptr), ctypes.c_void_p(t_ptr), int(nq), int(reps),
+                                   ctypes.byref(o), _P(ms)), "fc_autotune_batch")
+    return o, float(ms[0])
 
 
 def parse_edgelist(path: str, relabel: bool = False, nthreads: int = 0):

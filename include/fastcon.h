@@ -266,6 +266,18 @@ int fc_stcon_batch_noalloc(const int32_t *d_row_ptr, const int32_t *d_col, int32
                            const int32_t *d_t, int32_t nq, int32_t *d_connected, int32_t *d_hops,
                            int32_t sched, void *stream);
 
+/* Autotuner for repeated batches: runs the caller's sample batch (device
+ * arrays, as fc_stcon_batch_device) under each candidate setting of
+ * ctas_per_sm {2,3,4} x cta_work_k {2,4,8} x tile_entries {4096,8192,16384},
+ * `reps` timed runs each after a warm-up (1 <= reps <= 100), and writes the
+ * fastest into *inout (engine = FC_ENGINE_BATCHED; the schedule and the other
+ * fields are kept).  *best_ms (nullable) = its median kernel time.  No
+ * counterpart in the reference, whose launch shapes are compile-time
+ * constants (K/config.h, S/make_stcon.c:29-46). */
+int fc_autotune_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *d_graph_idx,
+                      const int32_t *d_s, const int32_t *d_t, int32_t nq, int32_t reps,
+                      fc_opts *inout, double *best_ms);
+
 /* ---- after the traversal: trees, paths, validation -------------------------- */
 /* BFS tree from s: parents[v] = the smallest-id in-neighbour of v one level
  * closer to s, parents[s] = s, -1 where unreachable (host array, nv).  The

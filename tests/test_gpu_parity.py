@@ -454,3 +454,24 @@ def test_first_call_after_workspace_growth(fastcon_lib, oracle_mod):
     assert (hops[samp] == want).all()
     conn2, hops2 = fc.stcon_batch(G, s, t, opts=opts(fc, "batched", "heuristic"))
     assert (hops2 == hops).all()
+
+
+# --------------------------------------------------------------------------
+# autotuner: picks one of its candidate settings; answers stay exact
+# --------------------------------------------------------------------------
+def test_autotune_batch(fastcon_lib, oracle_mod):
+    import torch
+    fc = fastcon_lib
+    u, v = graphs.rmat_edges(15, 8 << 15, seed=95, perm_seed=96)
+    G = fc.Graph.from_edges(u, v, 1 << 15)
+    rp, col = oracle_mod.build_csr(1 << 15, u, v)
+    s, t = graphs.pairs_with_degree(np.diff(rp), 300, seed=97)
+    _, want, _ = oracle_mod.stcon_batch(rp, col, s, t, nthreads=4)
+    ds = torch.from_numpy(s).cuda()
+    dt = torch.from_numpy(t).cuda()
+    o, ms = fc.autotune_batch(G, ds.data_ptr(), dt.data_ptr(), len(s), reps=1)
+    assert ms > 0 and o.engine == fc.ENGINE_BATCHED
+    assert o.ctas_per_sm in (2, 3, 4) and o.cta_work_k in (2, 4, 8)
+    assert o.tile_entries in (4096, 8192, 16384)
+    conn, hops = fc.stcon_batch(G, s, t, opts=o)
+    assert (hops == want).all()
