@@ -331,9 +331,12 @@ def run_fastcon(args, cfg):
 
     sched = {"heuristic": fc.SCHED_HEURISTIC, "plain": fc.SCHED_PLAIN,
              "learned": fc.SCHED_LEARNED}[args.sched]
-    if args.sched == "learned":
-        from fastcon import learn
+    from fastcon import learn
+    learned_ready = os.path.exists(learn.WEIGHTS_PATH)
+    if learned_ready:
         learn.load_default_weights()
+    elif args.sched == "learned":
+        raise SystemExit("learned schedule asked for but no weights at " + learn.WEIGHTS_PATH)
     Gs, gi, s, t = make_workload_gpu(fc, cfg)
     nq = len(s)
     # a dedicated stream: the library launches on it and the events record on it
@@ -404,6 +407,30 @@ def run_fastcon(args, cfg):
                 "kernel_ms": kms.tolist(), "kernel_alg_bytes": kbytes.tolist(),
                 "escalated_queries": esc}
 
+    # every schedule on the same device-resident workload (CUDA events)
+    schedules = {}
+    for name, sc in (("plain", fc.SCHED_PLAIN), ("heuristic", fc.SCHED_HEURISTIC),
+                     ("learned", fc.SCHED_LEARNED)):
+        if sc == fc.SCHED_LEARNED and not learned_ready:
+            continue
+        so = fc.make_opts(sched=sc, engine=fc.ENGINE_BATCHED, stream=stream.cuda_stream)
+        for _ in range(max(3, args.warmup)):
+            fc.stcon_batch_device(Gs, d_s.data_ptr(), d_t.data_ptr(), nq, d_c.data_ptr(),
+                                  d_h.data_ptr(), graph_idx_ptr=gptr, opts=so)
+        k = max(3, min(args.steps, 10))
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a0.record(stream)
+        for _ in range(k):
+            fc.stcon_batch_device(Gs, d_s.data_ptr(), d_t.data_ptr(), nq, d_c.data_ptr(),
+                                  d_h.data_ptr(), graph_idx_ptr=gptr, opts=so)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        sms = a0.elapsed_time(a1) / k
+        schedules[name] = {"value": nq / (sms / 1000.0), "unit": UNIT, "ms_per_step": sms,
+                           "exact": bool((d_h.cpu().numpy() == hops_gpu).all())}
+
     # e2e: host arrays (pinned), copies inside the timed region
     hs = torch.from_numpy(s).pin_memory().numpy()
     ht = torch.from_numpy(t).pin_memory().numpy()
@@ -417,7 +444,7 @@ def run_fastcon(args, cfg):
     e2e_s = reduce_over_ranks(ws, time.perf_counter() - t0, "max")
     e2e = {"value": total_q / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (8 if gi is None else 12) * nq,
            "d2h_bytes_per_step": 8 * nq}
-    exact = bool((hops == hops_gpu).all())
+    exact = bool((hops == hops_gpu).all()) and all(v["exact"] for v in schedules.values())
 
     # plain level-synchronous form and one-launch-per-query form, on samples
     plain_n = min(nq, 128 if cfg["kind"] != "grid" else 16)
@@ -469,7 +496,7 @@ def run_fastcon(args, cfg):
             # visited vertices counted once, i.e. half their degree sum
             "gteps_graph500": vadj / 2 / args.steps / (ms / args.steps / 1000.0) / 1e9,
             "edges_inspected_per_step": ins / args.steps,
-            "plain": plain, "one_launch_per_query": single,
+            "plain": plain, "one_launch_per_query": single, "schedules": schedules,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": launches * args.steps,
         }

@@ -318,12 +318,19 @@ __host__ __device__ inline void ql_apply_logits(QLocal &q, const float *o, int a
     const int side0 = q.side;
     if (q.two) {
         const float d = o[1] - o[0];
-        if (d > MLP_MARGIN) q.side = 1;
-        else if (d < -MLP_MARGIN) q.side = 0;
+        const int want = d > MLP_MARGIN ? 1 : (d < -MLP_MARGIN ? 0 : side0);
+        // trust region: the other side only while its step is at most twice
+        // the heuristic's (a wrong call then costs at most one such step)
+        const unsigned long long mw = q.dt[want] - q.dh[want];
+        const unsigned long long mh = q.dt[side0] - q.dh[side0];
+        if (want != side0 && mw <= 2 * mh + (unsigned long long)MLP_MIN_EDGES) q.side = want;
     }
     const float db = o[3] - o[2];
     const bool bu_ok = allow_bu && q.radius[q.side] + 1 <= bu_level_cap;
-    if (db > MLP_MARGIN && bu_ok)
+    // bottom-up scans every vertex: the network may turn a top-down step
+    // into one only for a frontier holding at least 1/64 of the entries
+    const bool bu_big = (long long)(q.dt[q.side] - q.dh[q.side]) * 64 >= q.ne;
+    if (db > MLP_MARGIN && bu_ok && (bu_big || (q.dir == DIR_BU && q.side == side0)))
         q.dir = DIR_BU;
     else if (db < -MLP_MARGIN || !bu_ok || q.side != side0)
         q.dir = DIR_TD;
