@@ -530,7 +530,7 @@ static int ensure_tmp(DevCtx *c)
 static int ensure_pool(DevCtx *c)
 {
     if (c->p_slots) return FC_OK;
-    int grid = pool_grid(c->sm_count, 0);
+    int grid = pool_max_grid(c->sm_count);
     if (grid <= 0 || !c->coop) {
         set_error("cooperative launch unavailable for the pool engine");
         return FC_ERR_UNSUPPORTED;
@@ -674,7 +674,7 @@ static int run_single(DevCtx *c, int mode, int engine, const GraphPairH &gp, int
         a.nlist = 1;
         a.out_conn = c->d_tmp_q + 2;
         a.out_hops = c->d_tmp_q + 3;
-        rc = pool_launch(a, c->p_grid, stream);
+        rc = pool_launch(a, pool_grid(c->sm_count, 0, 256), 256, stream);
         if (rc) return rc;
         rc = check_pool(c, stream, nullptr);
         if (rc) return rc;
@@ -817,7 +817,8 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         if ((rc = ensure_pool(c))) return rc;
         // three owner CTAs per SM (measured best on R-MAT-24 batches against 2
         // and 4); each owner costs a status array of the largest graph
-        int grid = pool_grid(c->sm_count, o.ctas_per_sm > 0 ? o.ctas_per_sm : 3);
+        const int block = pool_block(o.block);
+        int grid = pool_grid(c->sm_count, o.ctas_per_sm > 0 ? o.ctas_per_sm : 3, block);
         if (grid > c->p_grid) grid = c->p_grid;
         if (o.max_slots > 0 && o.max_slots < grid) grid = o.max_slots;
         // a slot's visit log bounds the queries it can finish itself; bigger
@@ -892,7 +893,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         auto issue = [&](unsigned evflags) -> int {
             FC_CUDA_TRY(cudaMemsetAsync(c->qstat, 0, sizeof(QueryStat) * (size_t)nq, stream));
             FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 8 * sizeof(int), stream));
-            int r = pool_launch(a, grid, stream);
+            int r = pool_launch(a, grid, block, stream);
             if (r) return r;
             FC_CUDA_TRY(cudaEventRecordWithFlags(c->evm, stream, evflags));
             return launch_persistent<T>(c, x, stream);
@@ -900,10 +901,10 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         if (o.use_graph) {
             // the two launches and their resets as one CUDA graph, replayed
             // while every argument (pointers, sizes, grids) stays the same
-            unsigned char key[sizeof(PoolArgs) + sizeof(PersistArgs) + 3 * sizeof(int)];
+            unsigned char key[sizeof(PoolArgs) + sizeof(PersistArgs) + 4 * sizeof(int)];
             std::memcpy(key, &a, sizeof(PoolArgs));
             std::memcpy(key + sizeof(PoolArgs), &x, sizeof(PersistArgs));
-            int tail[3] = {grid, xgrid, nq};
+            int tail[4] = {grid, xgrid, nq, block};
             std::memcpy(key + sizeof(PoolArgs) + sizeof(PersistArgs), tail, sizeof(tail));
             static_assert(sizeof(key) <= sizeof(c->gkey), "graph key too large");
             if (!(c->gexec && c->gkey_len == sizeof(key) &&

@@ -558,7 +558,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
 }
 
 template <int T>
-__global__ void __launch_bounds__(T, 4) k_pool(PoolArgs a)
+__global__ void __launch_bounds__(T, 1024 / T) k_pool(PoolArgs a)
 {
     __shared__ SmemPool<T> sm;
     const int tid = threadIdx.x;
@@ -615,10 +615,20 @@ __global__ void __launch_bounds__(T, 4) k_pool(PoolArgs a)
 size_t pool_slot_bytes() { return sizeof(PoolSlot); }
 size_t pool_job_bytes() { return sizeof(RowJob) * POOL_JOBS; }
 
-int pool_grid(int sm_count, int ctas_per_sm)
+// The pool kernel comes in CTAs of 128 and 256 threads; a batch picks one
+// (fc_opts.block), the single-query form uses 256.
+static const void *pool_kernel(int block)
 {
+    return block == 128 ? (const void *)k_pool<128> : (const void *)k_pool<256>;
+}
+
+int pool_block(int requested) { return requested == 128 ? 128 : 256; }
+
+int pool_grid(int sm_count, int ctas_per_sm, int block)
+{
+    block = pool_block(block);
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pool<FC_BLOCK>, FC_BLOCK, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pool_kernel(block), block, 0) !=
             cudaSuccess ||
         per_sm < 1)
         return 0;
@@ -626,12 +636,19 @@ int pool_grid(int sm_count, int ctas_per_sm)
     return per_sm * sm_count;
 }
 
-int pool_launch(const PoolArgs &a, int grid, cudaStream_t st)
+int pool_max_grid(int sm_count)
 {
+    const int a = pool_grid(sm_count, 0, 128), b = pool_grid(sm_count, 0, 256);
+    return a > b ? a : b;
+}
+
+int pool_launch(const PoolArgs &a, int grid, int block, cudaStream_t st)
+{
+    block = pool_block(block);
     PoolArgs args = a;
     void *kargs[] = {&args};
-    FC_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_pool<FC_BLOCK>, dim3(grid),
-                                            dim3(FC_BLOCK), kargs, 0, st));
+    FC_CUDA_TRY(cudaLaunchCooperativeKernel(pool_kernel(block), dim3(grid), dim3(block), kargs, 0,
+                                            st));
     return FC_OK;
 }
 

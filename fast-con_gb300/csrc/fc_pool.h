@@ -56,7 +56,9 @@ constexpr int TRACE_WORDS = 24;
 
 size_t pool_slot_bytes();
 size_t pool_job_bytes();  // per slot
-int pool_grid(int sm_count, int ctas_per_sm);
-int pool_launch(const PoolArgs &a, int grid, cudaStream_t st);
+int pool_block(int requested);                             // 128 or 256
+int pool_grid(int sm_count, int ctas_per_sm, int block);   // co-resident CTAs
+int pool_max_grid(int sm_count);                           // over both block sizes
+int pool_launch(const PoolArgs &a, int grid, int block, cudaStream_t st);
 
 }  // namespace fc
