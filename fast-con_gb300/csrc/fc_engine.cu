@@ -599,6 +599,7 @@ static PoolArgs pool_args_exclusive(DevCtx *c, int mode, const fc_opts &o)
     a.mode = mode;
     a.sched = o.sched;
     a.force_variant = forced_variant(o);
+    a.private_variant = -1;
     a.exclusive = 1;
     a.slots = (PoolSlot *)c->p_slots;
     a.jobs = (RowJob *)c->p_jobs;
@@ -849,6 +850,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.mode = MODE_STCON;
         a.sched = o.sched;
         a.force_variant = forced_variant(o);
+        a.private_variant = o.private_variant > 0 ? o.private_variant - 1 : -1;
         a.exclusive = 0;
         a.slots = (PoolSlot *)c->p_slots;
         a.jobs = (RowJob *)c->p_jobs;

@@ -447,6 +447,8 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
                     sm.ql.done = 1;
                 }
                 sm.publish = sm.ql.dir == DIR_BU || m > a.private_edges;
+                if (!sm.publish && a.private_variant >= 0 && a.force_variant < 0)
+                    sm.ql.variant = a.private_variant;
                 sm.t_step = global_timer_ns();
             }
         }

@@ -21,6 +21,7 @@ struct PoolArgs {
     const int *list_count;    // device count of list entries (nullable)
     int nlist;                // count when list_count is NULL
     int mode, sched, force_variant;
+    int private_variant;      // variant for steps the owner runs alone (-1: the schedule's)
     int exclusive;            // 1: CTA 0 owns every query in turn, arrays span the graph
     PoolSlot *slots;          // one per CTA
     RowJob *jobs;             // POOL_JOBS per CTA

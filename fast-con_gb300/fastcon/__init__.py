@@ -57,7 +57,7 @@ class Opts(ctypes.Structure):
                 ("max_slots", ctypes.c_int32), ("stream", ctypes.c_void_p),
                 ("cta_work_k", ctypes.c_int32), ("variant", ctypes.c_int32),
                 ("tile_entries", ctypes.c_int32), ("job_entries", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 4)]
+                ("private_variant", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
 class Stats(ctypes.Structure):
@@ -157,7 +157,7 @@ def _i32(a):
 
 def make_opts(sched=SCHED_HEURISTIC, engine=ENGINE_AUTO, block=0, ctas_per_sm=0, use_graph=0,
               max_slots=0, stream=None, cta_work_k=0, variant=0, tile_entries=0,
-              job_entries=0) -> Opts:
+              job_entries=0, private_variant=0) -> Opts:
     """variant: 0 = chosen by the schedule, 1 hybrid, 2 warp-centric, 3 lane per row;
     tile_entries / job_entries: work-sharing tile and row-job sizes (0 = defaults)."""
     o = Opts()
@@ -168,6 +168,7 @@ def make_opts(sched=SCHED_HEURISTIC, engine=ENGINE_AUTO, block=0, ctas_per_sm=0,
     o.cta_work_k = cta_work_k
     o.variant = variant
     o.tile_entries, o.job_entries = tile_entries, job_entries
+    o.private_variant = private_variant
     return o
 
 

@@ -78,7 +78,10 @@ typedef struct fc_opts {
     int32_t job_entries;  /* work-sharing engine: rows longer than this are
                              cut into jobs of this length (0 = 2048 for
                              batches, 8192 for one query on the grid)       */
-    int32_t reserved[4];
+    int32_t private_variant; /* work-sharing engine: expansion variant of the
+                             steps an owner CTA runs alone (same codes as
+                             `variant`; 0 = the schedule's choice)          */
+    int32_t reserved[3];
 } fc_opts;
 
 typedef struct fc_stats {
