@@ -119,7 +119,34 @@ struct SmemPool {
     unsigned seq, my_seq;
     int err;
     unsigned long long t_idle, t_step;
+    // the owner's query counters while it runs steps alone: shared-memory
+    // atomics and reads instead of global ones on every step's critical
+    // path; copied to the slot before a published step and back after it
+    TeamCounters stc;
 };
+
+// counters the helpers of a published step add to
+__device__ __forceinline__ void counters_to_slot(PoolSlot *my, const TeamCounters &c)
+{
+    for (int x = 0; x < 2; ++x) {
+        my->tc.tail[x] = c.tail[x];
+        my->tc.deg[x] = c.deg[x];
+        my->tc.hist[x] = c.hist[x];
+    }
+    my->tc.found = c.found;
+    my->tc.inspected = c.inspected;
+}
+
+__device__ __forceinline__ void counters_from_slot(TeamCounters &c, const PoolSlot *my)
+{
+    for (int x = 0; x < 2; ++x) {
+        c.tail[x] = ld_cg(&my->tc.tail[x]);
+        c.deg[x] = ld_cg_u64(&my->tc.deg[x]);
+        c.hist[x] = ld_cg_u64(&my->tc.hist[x]);
+    }
+    c.found = ld_cg(&my->tc.found);
+    c.inspected = ld_cg_u64(&my->tc.inspected);
+}
 
 // Expand the tile's rows (one per thread) with the step's variant; rows longer
 // than a row job go to the sink in every variant.
@@ -394,6 +421,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
         init_roots(a.mode, gp, s, t, status, levels, log, cap, &my->tc);
         __threadfence();
         ql_start(sm.ql, a.mode == MODE_STCON, nv, gp.fwd.ne, s, t, my->tc.deg[0], my->tc.deg[1]);
+        sm.stc = my->tc;
         sm.err = 0;
     }
     __syncthreads();
@@ -459,8 +487,8 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
         const int32_t *front = ql_frontier(sm.ql, log, cap, x, &F);
         if (!sm.publish) {
             run_step<T>(a.mode, gp, x, DIR_TD, sm.ql.radius[x], sm.ql.radius[1 - x], front, F, 0, 1,
-                        status, levels, log, cap, &my->tc.tail[x], &my->tc.deg[x], &my->tc.found,
-                        &my->tc.inspected, sm.td, sm.ql.variant, track ? &my->tc.hist[x] : nullptr);
+                        status, levels, log, cap, &sm.stc.tail[x], &sm.stc.deg[x], &sm.stc.found,
+                        &sm.stc.inspected, sm.td, sm.ql.variant, track ? &sm.stc.hist[x] : nullptr);
             __syncthreads();
         } else {
             desc.side = x;
@@ -490,17 +518,18 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             const int nvt = desc.dir == DIR_TD ? (int)(((long long)F + tv - 1) / tv)
                                                : (nv + POOL_TILE_V - 1) / POOL_TILE_V;
             desc.nvt = nvt;
+            if (tid == 0) counters_to_slot(my, sm.stc);  // published by the fence in the call
             pool_publish_and_run<T>(a, my, desc, nvt, sm);
             if (sm.err) return;
+            if (tid == 0) counters_from_slot(sm.stc, my);
         }
         if (tid == 0) {
             const unsigned long long ins0 = sm.ql.inspected;
             const int tail0 = sm.ql.tail[x], F0 = sm.ql.tail[x] - sm.ql.head[x];
             const int dir0 = sm.ql.dir, var0 = sm.ql.variant, step0 = sm.ql.steps;
-            ql_update(sm.ql, ld_cg(&my->tc.found), ld_cg(&my->tc.tail[x]), ld_cg_u64(&my->tc.deg[x]),
-                      ld_cg_u64(&my->tc.inspected));
+            ql_update(sm.ql, sm.stc.found, sm.stc.tail[x], sm.stc.deg[x], sm.stc.inspected);
             if (track) {
-                ql_update_hist(sm.ql, x, ld_cg_u64(&my->tc.hist[x]));
+                ql_update_hist(sm.ql, x, sm.stc.hist[x]);
             }
             if (a.trace) {
                 const int k = atomicAdd(a.trace_count, 1);
@@ -560,7 +589,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
 }
 
 template <int T>
-__global__ void __launch_bounds__(T, 1024 / T) k_pool(PoolArgs a)
+__global__ void __launch_bounds__(T, 768 / T) k_pool(PoolArgs a)
 {
     __shared__ SmemPool<T> sm;
     const int tid = threadIdx.x;

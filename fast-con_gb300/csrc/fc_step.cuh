@@ -25,6 +25,8 @@ namespace fc {
 
 constexpr int GATHER_PER_THREAD = 4;
 constexpr int BU_GROUP = 4;  // bottom-up: neighbours loaded together
+constexpr int TINY_STEP_E = 1024;  // a one-warp frontier reading at most this many entries
+                                   // is expanded by one warp without CTA barriers
 
 struct AppendTarget {
     int32_t *log;       // log base of the slot
@@ -242,14 +244,12 @@ __device__ __forceinline__ void expand_rows(const int32_t *__restrict__ col, int
                                             SmemTopDown<T> &sm, const Sink &sink)
 {
     const int tid = threadIdx.x, lane = tid & 31;
-    // class 1: rows of >= T entries, whole CTA (or row jobs for very long rows)
-    while (true) {
-        if (tid == 0) sm.owner = -1;
+    // class 1: rows of >= T entries, whole CTA (or row jobs for very long rows);
+    // one barrier when the tile has none
+    while (__syncthreads_or(re - rb >= T)) {
+        if (re - rb >= T) sm.owner = tid;  // any one of them
         __syncthreads();
-        if (re - rb >= T) sm.owner = tid;
-        __syncthreads();
-        int w = sm.owner;
-        if (w < 0) break;
+        const int w = sm.owner;
         if (tid == w) {
             if (sink.push_row(rb, re)) {
                 sm.rb = sm.re = 0;
@@ -413,6 +413,22 @@ __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t 
                              const int *stop_flag, const Sink &sink)
 {
     const int tid = threadIdx.x;
+    if (F <= 32 && team_size == 1) {
+        // a frontier of one warp's worth of short rows: that warp alone, no
+        // CTA barrier (the caller synchronises after the step); every warp
+        // reads the same rows and takes the same branch
+        const int lane = (int)lane_id();
+        int rb = 0, re = 0;
+        if (lane < F) {
+            const int u = ld_cg(frontier + lane);
+            rb = __ldg(row_ptr + u);
+            re = __ldg(row_ptr + u + 1);
+        }
+        if (warp_sum_i(re - rb) <= TINY_STEP_E) {
+            if (tid < 32) expand_warp(col, rb, re, vis, app, NoSink{}, INT_MAX);
+            return;
+        }
+    }
     for (long long base = (long long)team_rank * T; base < F; base += (long long)team_size * T) {
         int i = (int)base + tid;
         int rb = 0, re = 0;
@@ -422,7 +438,8 @@ __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t 
             re = __ldg(row_ptr + u + 1);
         }
         expand_rows<T>(col, rb, re, vis, app, sm, sink);
-        if (stop_flag) {
+        // the stop flag matters only when another tile of this CTA follows
+        if (stop_flag && base + (long long)team_size * T < F) {
             if (tid == 0) sm.stop = *(volatile const int *)stop_flag;
             __syncthreads();
             if (sm.stop) break;
