@@ -24,6 +24,7 @@
 namespace fc {
 
 constexpr int GATHER_PER_THREAD = 4;
+constexpr int WARP_ROW_MIN = 32;  // hybrid expansion: rows of at least this many entries go to a warp
 constexpr int BU_GROUP = 4;  // bottom-up: neighbours loaded together
 constexpr int TINY_STEP_E = 1024;  // a one-warp frontier reading at most this many entries
                                    // is expanded by one warp without CTA barriers
@@ -264,7 +265,7 @@ __device__ __forceinline__ void expand_rows(const int32_t *__restrict__ col, int
     }
     // class 2: rows of >= 32 entries, one warp
     while (true) {
-        unsigned m = __ballot_sync(0xffffffffu, re - rb >= 32);
+        unsigned m = __ballot_sync(0xffffffffu, re - rb >= WARP_ROW_MIN);
         if (!m) break;
         int leader = __ffs(m) - 1;
         int b = __shfl_sync(0xffffffffu, rb, leader);
