@@ -23,8 +23,8 @@
 
 namespace fc {
 
-constexpr int GATHER_PER_THREAD = 4;
-constexpr int WARP_ROW_MIN = 32;  // hybrid expansion: rows of at least this many entries go to a warp
+constexpr int GATHER_PER_THREAD = 8;
+constexpr int WARP_ROW_MIN = 128;  // hybrid expansion: rows of at least this many entries go to a warp
 constexpr int BU_GROUP = 4;  // bottom-up: neighbours loaded together
 constexpr int TINY_STEP_E = 1024;  // a one-warp frontier reading at most this many entries
                                    // is expanded by one warp without CTA barriers
