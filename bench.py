@@ -10,6 +10,10 @@ among vertices of degree >= 1 (seed 4).  One step = all queries of the
 workload through the library's batched engine.  The rmat24, grid4096 and
 batched512 graphs are larger than L2, so no L2 flush is added between steps.
 
+The headline schedule is the learned one (the metric's "learned+batched");
+`schedules` in the printed line gives plain, heuristic and learned on the same
+workload.
+
 Printed line (rank 0): value = queries/s with inputs resident in HBM (CUDA
 events on the launching stream); e2e = the same through fc_stcon_batch with
 pinned host arrays (copies inside the timed region); roofline of the
@@ -513,7 +517,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="fastcon", choices=["fastcon", "reference"])
     ap.add_argument("--config", default="rmat24", choices=sorted(CONFIGS))
-    ap.add_argument("--sched", default="heuristic", choices=["heuristic", "plain", "learned"])
+    ap.add_argument("--sched", default="learned", choices=["heuristic", "plain", "learned"])
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     import oracle
