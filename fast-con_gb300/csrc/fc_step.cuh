@@ -182,7 +182,13 @@ struct SmemTopDown {
     int warp_tot[T / 32];
     int total;
     int gather[T * GATHER_PER_THREAD];
+    int off[T];  // load-balanced search: exclusive prefix of the tile's row lengths
+    int rbs[T];  // and the rows' first entries
 };
+
+// Hybrid top-down expansion by load-balanced search (on) or by degree class
+// (off): see expand_lb and expand_rows.
+constexpr bool HYBRID_LB = true;
 
 // Block-wide inclusive scan of x; *total receives the sum.  All threads call.
 template <int T>
@@ -295,6 +301,59 @@ __device__ __forceinline__ void expand_rows(const int32_t *__restrict__ col, int
         warp_append<GATHER_PER_THREAD>(c, app);
         __syncthreads();
     }
+}
+
+// ---------------------------------------------------------------------------
+// Expand one tile by load-balanced search (after Merrill, Garland & Grimshaw's
+// scan-based gather and Gunrock's LB strategy): the tile's rows are laid end
+// to end by a CTA prefix scan, and entry e of that concatenation is read by
+// thread e mod T, which finds its row by binary search over the prefix in
+// shared memory.  Every thread reads GATHER_PER_THREAD entries per round
+// whatever the mix of row lengths, so a tile costs ceil(total / (T * K))
+// dependent rounds and three barriers; no row is walked by one warp or one
+// CTA alone.  Rows longer than the sink's job length go to the sink first.
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ __forceinline__ int lb_row(const int *off, int e)
+{
+    int lo = 0, hi = T;  // off[0] = 0 <= e: the last row starting at or before e
+#pragma unroll
+    for (int s = T / 2; s > 0; s >>= 1) {
+        const int mid = lo + s;
+        if (mid < hi && off[mid] <= e) lo = mid;
+    }
+    return lo;
+}
+
+template <int T, class Vis, class Sink>
+__device__ __forceinline__ void expand_lb(const int32_t *__restrict__ col, int rb, int re,
+                                          const Vis &vis, const AppendTarget &app,
+                                          SmemTopDown<T> &sm, const Sink &sink)
+{
+    const int tid = threadIdx.x;
+    if (re - rb > 0 && sink.push_row(rb, re)) rb = re;
+    const int d = re - rb;
+    const int incl = block_inclusive_scan<T>(d, sm.warp_tot, &sm.total);
+    sm.off[tid] = incl - d;
+    sm.rbs[tid] = rb;
+    __syncthreads();
+    const int total = sm.total;
+    constexpr int K = GATHER_PER_THREAD;
+    for (int base = 0; base < total; base += T * K) {
+        int v[K], c[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const int e = base + j * T + tid;
+            v[j] = -1;
+            if (e < total) {
+                const int r = lb_row<T>(sm.off, e);
+                v[j] = __ldg(col + sm.rbs[r] + (e - sm.off[r]));
+            }
+        }
+        visit_k<K>(vis, v, c);
+        warp_append<K>(c, app);
+    }
+    __syncthreads();  // the next tile rewrites off / rbs
 }
 
 // ---------------------------------------------------------------------------
@@ -438,7 +497,10 @@ __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t 
             rb = __ldg(row_ptr + u);
             re = __ldg(row_ptr + u + 1);
         }
-        expand_rows<T>(col, rb, re, vis, app, sm, sink);
+        if (HYBRID_LB)
+            expand_lb<T>(col, rb, re, vis, app, sm, sink);
+        else
+            expand_rows<T>(col, rb, re, vis, app, sm, sink);
         // the stop flag matters only when another tile of this CTA follows
         if (stop_flag && base + (long long)team_size * T < F) {
             if (tid == 0) sm.stop = *(volatile const int *)stop_flag;
