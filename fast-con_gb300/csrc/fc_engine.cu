@@ -57,6 +57,7 @@ struct StepArgs {
     unsigned long long *hist;  // degree-bin counters of the side (learned schedule)
     int2 *jobs;                // row jobs (rows over TEAM_SPLIT_E entries)
     int jcap;
+    int tile_v;                // frontier vertices per top-down tile
 };
 
 template <int T>
@@ -66,7 +67,7 @@ __global__ void __launch_bounds__(T) k_step(StepArgs a)
     run_step<T>(a.mode, a.gp, a.side, a.dir, a.level, a.other_radius, a.log + a.front_begin, a.F,
                 blockIdx.x, gridDim.x, a.status, a.levels, a.log, a.cap, &a.tc->tail[a.side],
                 &a.tc->deg[a.side], &a.tc->found, &a.tc->inspected, sm, a.variant, a.hist,
-                TeamSink{a.jobs, a.jcap, &a.tc->njobs[0], &a.tc->nok[0]});
+                TeamSink{a.jobs, a.jcap, &a.tc->njobs[0], &a.tc->nok[0]}, a.tile_v);
 }
 
 // The row jobs the preceding k_step left, on the whole grid.
@@ -165,7 +166,8 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
                         blockIdx.x, gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x],
                         &tc->deg[x], &tc->found, &tc->inspected, sm, ql.variant,
                         a.mlp ? &tc->hist[x] : nullptr,
-                        TeamSink{a.jobs, a.jcap, &tc->njobs[par], &tc->nok[par]});
+                        TeamSink{a.jobs, a.jcap, &tc->njobs[par], &tc->nok[par]},
+                        team_tile_v<T>(F, (long long)(ql.dt[x] - ql.dh[x])));
             if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
             if (ql.dir == DIR_TD) {
                 __shared__ int s_nj;
@@ -411,7 +413,8 @@ static int hostloop(DevCtx *c, int mode, const GraphPairH &gph, int s, int t, in
         a.hist = learned ? &c->tc->hist[x] : nullptr;
         a.jobs = c->tjobs;
         a.jcap = c->tjobs_cap;
-        int grid = q.dir == DIR_TD ? (a.F + T - 1) / T : full_grid;
+        a.tile_v = team_tile_v<T>(a.F, (long long)(q.dt[x] - q.dh[x]));
+        int grid = q.dir == DIR_TD ? (a.F + a.tile_v - 1) / a.tile_v : full_grid;
         if (grid > full_grid) grid = full_grid;
         if (grid < 1) grid = 1;
         // rows over TEAM_SPLIT_E entries become row jobs for a second,

@@ -159,10 +159,8 @@ __device__ __forceinline__ void pool_expand(int variant, const int32_t *__restri
         expand_warp(col, rb, re, vis, app, sink, sink.split);
     else if (variant == VAR_THREAD)
         expand_thread(col, rb, re, vis, app, sink, sink.split);
-    else if (HYBRID_LB)
-        expand_lb<T>(col, rb, re, vis, app, td, sink);
     else
-        expand_rows<T>(col, rb, re, vis, app, td, sink);
+        expand_lb<T>(col, rb, re, vis, app, td, sink);
 }
 
 // ---------------------------------------------------------------------------

@@ -369,7 +369,8 @@ __device__ __forceinline__ void topdown_variant(int variant, const DGraph &gx,
                                                 const int32_t *frontier, int F, int team_rank,
                                                 int team_size, const Vis &vis,
                                                 const AppendTarget &app, SmemTopDown<T> &sm,
-                                                const int *stop, const TeamSink &sink)
+                                                const int *stop, const TeamSink &sink,
+                                                int tile_v = T)
 {
     if (variant == VAR_WARP)
         topdown_warps<T, VAR_WARP>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis,
@@ -379,7 +380,7 @@ __device__ __forceinline__ void topdown_variant(int variant, const DGraph &gx,
                                      app, stop, sink);
     else
         topdown_step<T>(gx.row_ptr, gx.col, frontier, F, team_rank, team_size, vis, app, sm, stop,
-                        sink);
+                        sink, tile_v);
 }
 
 template <int T>
@@ -389,7 +390,8 @@ __device__ void run_step(int mode, const GraphPair &gp, int side, int dir, int l
                          int *tail_ctr, unsigned long long *deg_ctr, int *found,
                          unsigned long long *bu_ins, SmemTopDown<T> &sm, int variant = VAR_HYBRID,
                          unsigned long long *hist = nullptr,
-                         TeamSink sink = TeamSink{nullptr, 0, nullptr, nullptr})
+                         TeamSink sink = TeamSink{nullptr, 0, nullptr, nullptr},
+                         int tile_v = T)
 {
     const DGraph &gx = side ? gp.rev : gp.fwd;
     AppendTarget app{log, cap, side, tail_ctr, deg_ctr, gx.row_ptr, hist};
@@ -397,11 +399,11 @@ __device__ void run_step(int mode, const GraphPair &gp, int side, int dir, int l
         if (mode == MODE_BFS) {
             VisitBFS vis{levels, level + 1};
             topdown_variant<T>(variant, gx, frontier, F, team_rank, team_size, vis, app, sm,
-                               nullptr, sink);
+                               nullptr, sink, tile_v);
         } else {
             VisitSTCON vis{status, st_code(side, level + 1), side, found};
             topdown_variant<T>(variant, gx, frontier, F, team_rank, team_size, vis, app, sm, found,
-                               sink);
+                               sink, tile_v);
         }
     } else {
         const DGraph &gr = side ? gp.fwd : gp.rev;

@@ -6,15 +6,16 @@
 // take the team rank/size and never synchronise across CTAs themselves; the
 // engine puts a team barrier between steps.
 //
-// Top-down expansion balances load by degree class (after Merrill, Garland &
-// Grimshaw, "Scalable GPU Graph Traversal", PPoPP 2012):
-//   rows >= BLOCK entries   -> the whole CTA walks the row
-//   rows >= 32 entries      -> one warp walks the row
-//   smaller rows            -> CTA prefix scan of the degrees, the row offsets are
-//                              staged in shared memory and gathered by all threads
-// Rows are walked with 16-byte int4 loads of the column array (scalar loads only
-// for the unaligned head and tail).  Newly claimed vertices are appended to the
-// log with a warp ballot/shuffle scan and one atomicAdd per warp.
+// Top-down expansion (the hybrid variant) reads a tile's rows by load-balanced
+// search: a CTA prefix scan lays the rows end to end and every thread reads
+// GATHER_PER_THREAD entries per round, finding each entry's row by binary
+// search in shared memory, whatever the mix of row lengths (after Merrill,
+// Garland & Grimshaw, "Scalable GPU Graph Traversal", PPoPP 2012, and the
+// load-balanced strategy of Gunrock).  Rows longer than the engine's job
+// length become row jobs that the whole team shares.  Long rows in the other
+// variants are walked with 16-byte int4 loads of the column array.  Newly
+// claimed vertices are appended to the log with a warp ballot/shuffle scan
+// and one atomicAdd per warp.
 #pragma once
 
 #include <climits>
@@ -23,8 +24,21 @@
 
 namespace fc {
 
-constexpr int GATHER_PER_THREAD = 8;
-constexpr int WARP_ROW_MIN = 128;  // hybrid expansion: rows of at least this many entries go to a warp
+constexpr int GATHER_PER_THREAD = 8;  // load-balanced search: entries per thread per round
+constexpr long long TEAM_TILE_E = 16384;  // team steps: adjacency entries a tile aims at
+
+// Frontier vertices per top-down tile of a team step: T, or fewer (a power
+// of two, at least 1) when the frontier's m entries over F vertices would
+// give tiles of more than TEAM_TILE_E entries.
+template <int T>
+__host__ __device__ inline int team_tile_v(long long F, long long m)
+{
+    if (F <= 0 || m <= (long long)F * (TEAM_TILE_E / T)) return T;
+    const long long want = TEAM_TILE_E * F / m;
+    int tv = 1;
+    while (tv * 2 <= want && tv * 2 <= T) tv *= 2;
+    return tv;
+}
 constexpr int BU_GROUP = 4;  // bottom-up: neighbours loaded together
 constexpr int TINY_STEP_E = 1024;  // a one-warp frontier reading at most this many entries
                                    // is expanded by one warp without CTA barriers
@@ -176,19 +190,12 @@ __device__ __forceinline__ void walk_range(const int32_t *__restrict__ col, int 
 
 template <int T>
 struct SmemTopDown {
-    int owner;
-    int rb, re;
     int stop;
     int warp_tot[T / 32];
     int total;
-    int gather[T * GATHER_PER_THREAD];
     int off[T];  // load-balanced search: exclusive prefix of the tile's row lengths
     int rbs[T];  // and the rows' first entries
 };
-
-// Hybrid top-down expansion by load-balanced search (on) or by degree class
-// (off): see expand_lb and expand_rows.
-constexpr bool HYBRID_LB = true;
 
 // Block-wide inclusive scan of x; *total receives the sum.  All threads call.
 template <int T>
@@ -240,68 +247,6 @@ struct TeamSink {
         return true;
     }
 };
-
-// ---------------------------------------------------------------------------
-// Expand one tile of frontier vertices; thread tid holds the row [rb, re) of
-// its vertex (empty when it has none).  All threads of the CTA call it.
-// ---------------------------------------------------------------------------
-template <int T, class Vis, class Sink>
-__device__ __forceinline__ void expand_rows(const int32_t *__restrict__ col, int rb, int re,
-                                            const Vis &vis, const AppendTarget &app,
-                                            SmemTopDown<T> &sm, const Sink &sink)
-{
-    const int tid = threadIdx.x, lane = tid & 31;
-    // class 1: rows of >= T entries, whole CTA (or row jobs for very long rows);
-    // one barrier when the tile has none
-    while (__syncthreads_or(re - rb >= T)) {
-        if (re - rb >= T) sm.owner = tid;  // any one of them
-        __syncthreads();
-        const int w = sm.owner;
-        if (tid == w) {
-            if (sink.push_row(rb, re)) {
-                sm.rb = sm.re = 0;
-            } else {
-                sm.rb = rb;
-                sm.re = re;
-            }
-            rb = re;
-        }
-        __syncthreads();
-        walk_range(col, sm.rb, sm.re, tid, T, vis, app);
-    }
-    // class 2: rows of >= 32 entries, one warp
-    while (true) {
-        unsigned m = __ballot_sync(0xffffffffu, re - rb >= WARP_ROW_MIN);
-        if (!m) break;
-        int leader = __ffs(m) - 1;
-        int b = __shfl_sync(0xffffffffu, rb, leader);
-        int e = __shfl_sync(0xffffffffu, re, leader);
-        if (lane == leader) rb = re;
-        walk_range(col, b, e, lane, 32, vis, app);
-    }
-    // class 3: short rows, CTA scan + shared-memory gather
-    int d = re - rb;
-    int incl = block_inclusive_scan<T>(d, sm.warp_tot, &sm.total);
-    int off = incl - d;
-    const int total = sm.total;
-    constexpr int G = T * GATHER_PER_THREAD;
-    for (int chunk = 0; chunk < total; chunk += G) {
-        int lo = max(off, chunk), hi = min(off + d, chunk + G);
-        for (int j = lo; j < hi; ++j) sm.gather[j - chunk] = rb + (j - off);
-        __syncthreads();
-        const int cnt = min(G, total - chunk);
-        // GATHER_PER_THREAD entries per thread, all loads in flight together
-        int v[GATHER_PER_THREAD], c[GATHER_PER_THREAD];
-#pragma unroll
-        for (int j = 0; j < GATHER_PER_THREAD; ++j) {
-            const int k = j * T + tid;
-            v[j] = k < cnt ? __ldg(col + sm.gather[k]) : -1;
-        }
-        visit_k<GATHER_PER_THREAD>(vis, v, c);
-        warp_append<GATHER_PER_THREAD>(c, app);
-        __syncthreads();
-    }
-}
 
 // ---------------------------------------------------------------------------
 // Expand one tile by load-balanced search (after Merrill, Garland & Grimshaw's
@@ -470,7 +415,7 @@ template <int T, class Vis, class Sink>
 __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
                              const int32_t *frontier, int F, int team_rank, int team_size,
                              const Vis &vis, const AppendTarget &app, SmemTopDown<T> &sm,
-                             const int *stop_flag, const Sink &sink)
+                             const int *stop_flag, const Sink &sink, int tile_v = T)
 {
     const int tid = threadIdx.x;
     if (F <= 32 && team_size == 1) {
@@ -489,20 +434,20 @@ __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t 
             return;
         }
     }
-    for (long long base = (long long)team_rank * T; base < F; base += (long long)team_size * T) {
-        int i = (int)base + tid;
+    // tiles of tile_v (<= T) frontier vertices, one per thread, dealt
+    // round-robin: frontiers of high degree get tiles of fewer vertices
+    const long long step = (long long)team_size * tile_v;
+    for (long long base = (long long)team_rank * tile_v; base < F; base += step) {
+        const long long i = base + tid;
         int rb = 0, re = 0;
-        if (i < F) {
+        if (tid < tile_v && i < F) {
             int u = ld_cg(frontier + i);
             rb = __ldg(row_ptr + u);
             re = __ldg(row_ptr + u + 1);
         }
-        if (HYBRID_LB)
-            expand_lb<T>(col, rb, re, vis, app, sm, sink);
-        else
-            expand_rows<T>(col, rb, re, vis, app, sm, sink);
+        expand_lb<T>(col, rb, re, vis, app, sm, sink);
         // the stop flag matters only when another tile of this CTA follows
-        if (stop_flag && base + (long long)team_size * T < F) {
+        if (stop_flag && base + step < F) {
             if (tid == 0) sm.stop = *(volatile const int *)stop_flag;
             __syncthreads();
             if (sm.stop) break;
