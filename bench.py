@@ -346,7 +346,10 @@ def run_fastcon(args, cfg):
     # a dedicated stream: the library launches on it and the events record on it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    opt = fc.make_opts(sched=sched, engine=fc.ENGINE_BATCHED, stream=stream.cuda_stream)
+    # repeated batches of one shape: the library replays one captured CUDA
+    # graph per batch (use_graph), as a serving loop would
+    opt = fc.make_opts(sched=sched, engine=fc.ENGINE_BATCHED, stream=stream.cuda_stream,
+                       use_graph=1)
     d_s = torch.from_numpy(s).cuda()
     d_t = torch.from_numpy(t).cuda()
     d_g = torch.from_numpy(gi).cuda() if gi is not None else None
@@ -439,7 +442,7 @@ def run_fastcon(args, cfg):
     hs = torch.from_numpy(s).pin_memory().numpy()
     ht = torch.from_numpy(t).pin_memory().numpy()
     hg = torch.from_numpy(gi).pin_memory().numpy() if gi is not None else None
-    e2e_opt = fc.make_opts(sched=sched, engine=fc.ENGINE_BATCHED)
+    e2e_opt = fc.make_opts(sched=sched, engine=fc.ENGINE_BATCHED, use_graph=1)
     fc.stcon_batch(Gs, hs, ht, graph_idx=hg, opts=e2e_opt)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
