@@ -173,20 +173,23 @@ __device__ __forceinline__ void walk_range(const int32_t *__restrict__ col, int 
             c[0] = vis.visit(__ldg(col + z + lane_idx - nhead));
         warp_append<1>(c, app);
     }
+    // two 16-byte loads per lane and round: 8 neighbours' probes in flight
     const int4 *col4 = reinterpret_cast<const int4 *>(col);
     const int k_end = z >> 2;
-    for (int k0 = a >> 2; k0 < k_end; k0 += nlanes) {
-        int k = k0 + lane_idx;
-        int v[4] = {-1, -1, -1, -1}, c[4];
-        if (k < k_end) {
-            int4 x = __ldg(col4 + k);
-            v[0] = x.x;
-            v[1] = x.y;
-            v[2] = x.z;
-            v[3] = x.w;
+    for (int k0 = a >> 2; k0 < k_end; k0 += 2 * nlanes) {
+        int v[8], c[8];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int k = k0 + h * nlanes + lane_idx;
+            int4 x = make_int4(-1, -1, -1, -1);
+            if (k < k_end) x = __ldg(col4 + k);
+            v[4 * h + 0] = x.x;
+            v[4 * h + 1] = x.y;
+            v[4 * h + 2] = x.z;
+            v[4 * h + 3] = x.w;
         }
-        visit_k<4>(vis, v, c);
-        warp_append<4>(c, app);
+        visit_k<8>(vis, v, c);
+        warp_append<8>(c, app);
     }
 }
 
