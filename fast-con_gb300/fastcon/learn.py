@@ -322,8 +322,8 @@ def policy_regret(X, C, A, P, w=None):
         hd = np.array([CANDIDATES[a][1] for a in A])
         ds = z[:, 1] - z[:, 0]
         side = np.where(ds > MARGIN, 1, np.where(ds < -MARGIN, 0, hs))
-        db = z[:, 3] - z[:, 2]
-        bu = np.where(db > MARGIN, 1, np.where((db < -MARGIN) | (side != hs), 0, hd))
+        # the device keeps the heuristic's direction (top-down after a side change)
+        bu = np.where(side != hs, 0, hd)
         act = np.array([CANDIDATES.index((int(a), int(b))) for a, b in zip(side, bu)])
     chosen = C[np.arange(len(C)), act]
     return float(chosen.sum() / max(best.sum(), 1.0) - 1.0)

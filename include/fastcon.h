@@ -46,8 +46,9 @@ extern "C" {
 #define FC_SCHED_HEURISTIC 1  /* side with the smaller frontier-edge sum first;
                                  bottom-up when the frontier's edges exceed the
                                  unexplored edges / 14 (fixed thresholds)               */
-#define FC_SCHED_LEARNED   2  /* MLP chooses side x direction x variant; uses the
-                                 heuristic until weights are loaded                    */
+#define FC_SCHED_LEARNED   2  /* MLP chooses the side (heads for direction and
+                                 variant are trained, not applied); the heuristic
+                                 until weights are loaded                              */
 
 /* ---- execution engines ------------------------------------------------- */
 #define FC_ENGINE_AUTO       0
@@ -216,8 +217,10 @@ int fc_stcon_batch_device(fc_graph *const *gs, int32_t ngraphs, const int32_t *d
  * 1,703 floats, W1[32][12] b1[32] W2[32][32] b2[32] W3[7][32] b3[7], or
  * 1,727 = those followed by the training feature box lo[12], hi[12] (steps
  * whose features fall outside it are left to the heuristic).  Logits 0-1
- * pick the side, 2-3 top-down / bottom-up, 4-6 the expansion variant; a head
- * overrides the heuristic only with a logit margin above ln 3.  The network
+ * pick the side, 2-3 top-down / bottom-up, 4-6 the expansion variant.  Only
+ * the side head is applied, with a logit margin above ln 3 and while the
+ * other side's step reads at most twice the heuristic's; direction and
+ * variant stay the heuristic's.  The network
  * reads 12 features per step (frontier sizes and adjacency sums of both
  * sides scaled by the graph size, unexplored fraction, last side, frontier
  * degree mix, radii).  fc_sched_get_weights copies n (1,703 or 1,727). */
