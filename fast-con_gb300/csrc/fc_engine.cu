@@ -193,11 +193,8 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
         if (a.mode == MODE_STCON) {
             // clear exactly the claimed vertices (the log holds each once)
             const int n0 = ql.tail[0], n1 = ql.tail[1];
-            for (long long i = (long long)blockIdx.x * T + threadIdx.x; i < n0 + n1;
-                 i += (long long)gridDim.x * T) {
-                int v = i < n0 ? a.log[i] : a.log[nv - 1 - (i - n0)];
-                a.status[v] = ST_UNVISITED;
-            }
+            clear_claimed(a.status, a.log, nv, n0, 0, (long long)n0 + n1,
+                          (long long)blockIdx.x * T + threadIdx.x, (long long)gridDim.x * T);
         }
         if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
     }

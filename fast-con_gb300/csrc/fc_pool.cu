@@ -175,10 +175,7 @@ __device__ void pool_tile(const PoolArgs &a, PoolSlot *slot, int tile, unsigned 
     if (d.dir == DIR_RESET) {
         const int n0 = d.F;  // entries of side 0; the rest belong to side 1
         const int lo = tile * POOL_TILE_R, hi = min(d.nreset, lo + POOL_TILE_R);
-        for (int i = lo + tid; i < hi; i += T) {
-            int v = i < n0 ? d.log[i] : d.log[d.cap - 1 - (i - n0)];
-            d.status[v] = ST_UNVISITED;
-        }
+        clear_claimed(d.status, d.log, d.cap, n0, lo, hi, tid, T);
         return;
     }
     // already met: skip the tile (one read, shared, so the whole CTA agrees)
@@ -567,10 +564,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
     if (a.mode == MODE_STCON) {
         const int n0 = sm.ql.tail[0], n1 = sm.ql.tail[1];
         if (n0 + n1 <= 4 * POOL_TILE_R) {
-            for (int i = tid; i < n0 + n1; i += T) {
-                int v = i < n0 ? log[i] : log[cap - 1 - (i - n0)];
-                status[v] = ST_UNVISITED;
-            }
+            clear_claimed(status, log, cap, n0, 0, (long long)n0 + n1, tid, T);
         } else {
             desc.F = n0;
             desc.dir = DIR_RESET;

@@ -480,6 +480,29 @@ __device__ void team_jobs(const int32_t *__restrict__ col, const int2 *jobs, int
     }
 }
 
+// Clear the status bytes of the claimed vertices in log entries [lo, hi)
+// (entries below n0 are side 0's, read from the front; the rest side 1's,
+// read from the back of the log), thread `first` of `stride`.  Eight log
+// reads are in flight per thread before its stores: a byte store may alias
+// the log as far as the compiler knows, so a plain loop waits for every
+// read in turn.
+__device__ __forceinline__ void clear_claimed(uint8_t *status, const int32_t *log, int cap,
+                                              long long n0, long long lo, long long hi,
+                                              long long first, long long stride)
+{
+    for (long long base = lo + first; base < hi; base += 8 * stride) {
+        int v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const long long i = base + k * stride;
+            v[k] = i < hi ? __ldcg(i < n0 ? log + i : log + (cap - 1 - (i - n0))) : -1;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (v[k] >= 0) status[v[k]] = ST_UNVISITED;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Bottom-up step.  Every vertex v of [0, nv) not yet owned by the expanding
 // side scans its (reverse-graph) neighbours for one in the expanding side's
