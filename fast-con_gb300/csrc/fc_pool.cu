@@ -118,6 +118,7 @@ struct SmemPool {
     int q, li, publish, flag, cand, claimed, cursor;
     unsigned seq, my_seq;
     int err;
+    unsigned backoff;  // idle polling pause, ns
     unsigned long long t_idle, t_step;
     // the owner's query counters while it runs steps alone: shared-memory
     // atomics and reads instead of global ones on every step's critical
@@ -612,8 +613,13 @@ __global__ void __launch_bounds__(T, 768 / T) k_pool(PoolArgs a)
             if (sm.err) break;
         }
     }
-    // help until every query is finished
-    if (tid == 0) sm.t_idle = global_timer_ns();
+    // help until every query is finished; an idle CTA polls the slots with a
+    // growing pause (128 ns to 4 us) so that the pollers of the batch's tail
+    // do not crowd the L2 lines the working CTAs claim tiles from
+    if (tid == 0) {
+        sm.t_idle = global_timer_ns();
+        sm.backoff = 128;
+    }
     __syncthreads();
     while (true) {
         if (tid == 0) {
@@ -626,9 +632,13 @@ __global__ void __launch_bounds__(T, 768 / T) k_pool(PoolArgs a)
         __syncthreads();
         if (sm.flag) break;
         if (pool_steal<T>(a, sm)) {
-            if (tid == 0) sm.t_idle = global_timer_ns();
+            if (tid == 0) {
+                sm.t_idle = global_timer_ns();
+                sm.backoff = 128;
+            }
         } else if (tid == 0) {
-            __nanosleep(256);
+            __nanosleep(sm.backoff);
+            if (sm.backoff < 4096) sm.backoff *= 2;
         }
         __syncthreads();
     }
