@@ -118,6 +118,8 @@ struct SmemPool {
     int q, li, publish, flag, cand, claimed, cursor;
     unsigned seq, my_seq;
     int err;
+    int nq;            // queries of the launch
+    int tail;          // every query has an owner: idle CTAs are about
     unsigned backoff;  // idle polling pause, ns
     unsigned long long t_idle, t_step;
     // the owner's query counters while it runs steps alone: shared-memory
@@ -472,7 +474,11 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
                     sm.ql.escalate = 1;  // the log could overflow: finish it in exclusive mode
                     sm.ql.done = 1;
                 }
-                sm.publish = sm.ql.dir == DIR_BU || m > a.private_edges;
+                // in the batch's tail (every query taken, idle CTAs about)
+                // smaller steps are shared, in smaller tiles
+                sm.tail = !a.exclusive && ld_cg(&a.ctr[CTR_NEXT]) >= sm.nq;
+                const long long priv = sm.tail ? a.private_edges / 8 : a.private_edges;
+                sm.publish = sm.ql.dir == DIR_BU || m > priv;
                 if (!sm.publish && a.private_variant >= 0 && a.force_variant < 0)
                     sm.ql.variant = a.private_variant;
                 sm.t_step = global_timer_ns();
@@ -503,8 +509,9 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             // than about 8 tiles per CTA (fewer claims on the slot word)
             const long long m = (long long)(sm.ql.dt[x] - sm.ql.dh[x]);
             int tv = T;
-            if (m > (long long)F * (a.tile_e / T)) {
-                const long long want_v = (long long)a.tile_e * F / (m > 0 ? m : 1);
+            const int tile_e = sm.tail ? max(a.tile_e / 4, 2 * T) : a.tile_e;
+            if (m > (long long)F * (tile_e / T)) {
+                const long long want_v = (long long)tile_e * F / (m > 0 ? m : 1);
                 tv = 1;
                 while (tv * 2 <= want_v) tv *= 2;
             } else {
@@ -591,6 +598,8 @@ __global__ void __launch_bounds__(T, 768 / T) k_pool(PoolArgs a)
     PoolSlot *my = a.slots + blockIdx.x;
     const int nq = a.list_count ? ld_cg(a.list_count) : a.nlist;
     if (tid == 0) {
+        sm.nq = nq;
+        sm.tail = 0;
         sm.cursor = (int)((blockIdx.x * 97u) % gridDim.x);
         sm.li = 0;
         sm.err = 0;
