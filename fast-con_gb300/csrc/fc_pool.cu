@@ -156,14 +156,15 @@ __device__ __forceinline__ void counters_from_slot(TeamCounters &c, const PoolSl
 template <int T, class Vis>
 __device__ __forceinline__ void pool_expand(int variant, const int32_t *__restrict__ col, int rb,
                                             int re, const Vis &vis, const AppendTarget &app,
-                                            SmemTopDown<T> &td, const SlotSink &sink)
+                                            SmemTopDown<T> &td, const SlotSink &sink,
+                                            const int *stop)
 {
     if (variant == VAR_WARP)
         expand_warp(col, rb, re, vis, app, sink, sink.split);
     else if (variant == VAR_THREAD)
         expand_thread(col, rb, re, vis, app, sink, sink.split);
     else
-        expand_lb<T>(col, rb, re, vis, app, td, sink);
+        expand_lb<T>(col, rb, re, vis, app, td, sink, stop);
 }
 
 // ---------------------------------------------------------------------------
@@ -236,10 +237,10 @@ __device__ void pool_tile(const PoolArgs &a, PoolSlot *slot, int tile, unsigned 
             }
             if (d.mode == MODE_BFS) {
                 VisitBFS vis{d.levels, d.level + 1};
-                pool_expand<T>(d.variant, gx.col, rb, re, vis, app, sm.td, sink);
+                pool_expand<T>(d.variant, gx.col, rb, re, vis, app, sm.td, sink, nullptr);
             } else {
                 VisitSTCON vis{d.status, st_code(d.side, d.level + 1), d.side, &slot->tc.found};
-                pool_expand<T>(d.variant, gx.col, rb, re, vis, app, sm.td, sink);
+                pool_expand<T>(d.variant, gx.col, rb, re, vis, app, sm.td, sink, &slot->tc.found);
             }
         }
         return;

@@ -278,7 +278,8 @@ __device__ __forceinline__ int lb_row(const int *off, int e)
 template <int T, class Vis, class Sink, int K = GATHER_PER_THREAD>
 __device__ __forceinline__ void expand_lb(const int32_t *__restrict__ col, int rb, int re,
                                           const Vis &vis, const AppendTarget &app,
-                                          SmemTopDown<T> &sm, const Sink &sink)
+                                          SmemTopDown<T> &sm, const Sink &sink,
+                                          const int *stop = nullptr)
 {
     const int tid = threadIdx.x;
     if (re - rb > 0 && sink.push_row(rb, re)) rb = re;
@@ -289,6 +290,9 @@ __device__ __forceinline__ void expand_lb(const int32_t *__restrict__ col, int r
     __syncthreads();
     const int total = sm.total;
     for (int base = 0; base < total; base += T * K) {
+        // a set stop flag (the sides met) ends the tile within one round;
+        // the test is warp-uniform, the rounds hold no CTA barrier
+        if (stop && base > 0 && __any_sync(0xffffffffu, *(volatile const int *)stop != 0)) break;
         int v[K], c[K];
 #pragma unroll
         for (int j = 0; j < K; ++j) {
@@ -450,9 +454,9 @@ __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t 
             re = __ldg(row_ptr + u + 1);
         }
         if (team_size > 1)
-            expand_lb<T, Vis, Sink, GATHER_TEAM>(col, rb, re, vis, app, sm, sink);
+            expand_lb<T, Vis, Sink, GATHER_TEAM>(col, rb, re, vis, app, sm, sink, stop_flag);
         else
-            expand_lb<T>(col, rb, re, vis, app, sm, sink);
+            expand_lb<T>(col, rb, re, vis, app, sm, sink, stop_flag);
         // the stop flag matters only when another tile of this CTA follows
         if (stop_flag && base + step < F) {
             if (tid == 0) sm.stop = *(volatile const int *)stop_flag;
