@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(T) k_rowjobs(StepArgs a)
     const int nj = min(*(volatile const int *)&a.tc->nok[0], a.jcap);
     run_team_jobs<T>(a.mode, a.gp, a.side, a.level, a.jobs, nj, blockIdx.x, gridDim.x, a.status,
                      a.levels, a.log, a.cap, &a.tc->tail[a.side], &a.tc->deg[a.side],
-                     &a.tc->found, sm, a.hist);
+                     &a.tc->found, sm, a.hist, &a.tc->inspected);
 }
 
 // ---------------------------------------------------------------------------
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
                 if (s_nj > 0) {  // same value in every CTA: uniform barrier
                     run_team_jobs<T>(a.mode, gp, x, ql.radius[x], a.jobs, s_nj, blockIdx.x,
                                      gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x],
-                                     &tc->deg[x], &tc->found, sm, a.mlp ? &tc->hist[x] : nullptr);
+                                     &tc->deg[x], &tc->found, sm, a.mlp ? &tc->hist[x] : nullptr, &tc->inspected);
                     if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
                 }
             }

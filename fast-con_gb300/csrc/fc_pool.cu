@@ -190,7 +190,7 @@ __device__ void pool_tile(const PoolArgs &a, PoolSlot *slot, int tile, unsigned 
     const GraphPair &gp = a.graphs[d.gidx];
     const DGraph &gx = d.side ? gp.rev : gp.fwd;
     AppendTarget app{d.log, d.cap, d.side, &slot->tc.tail[d.side], &slot->tc.deg[d.side],
-                     gx.row_ptr, d.track_hist ? &slot->tc.hist[d.side] : nullptr};
+                     gx.row_ptr, d.track_hist ? &slot->tc.hist[d.side] : nullptr, &slot->tc.inspected};
     if (tile >= d.nvt) {
         // row job: wait (bounded) until its descriptor carries this step's seq
         RowJob *J = a.jobs + (size_t)(slot - a.slots) * POOL_JOBS + (tile - d.nvt);

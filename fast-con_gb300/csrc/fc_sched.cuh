@@ -153,13 +153,14 @@ __host__ __device__ inline void ql_update(QLocal &q, int found, int tail_x,
     //   top-down   4|F| + 8|F| + 4 E_F + 4 E_F + 4|N| + 4|N|
     //   bottom-up  sum over scanned v of (4 + 8 + 8 k_v), plus 8|N|
     const unsigned long long nnew = (unsigned long long)(tail_x - q.tail[x]);
+    // entries actually read (the steps add them to one counter): a meeting
+    // step that stops early reads fewer than its frontier's degree sum
+    const unsigned long long k = bu_total - q.bu_seen;
     if (q.dir == DIR_TD) {
-        const unsigned long long ef = q.dt[x] - q.dh[x];
         const unsigned long long nf = (unsigned long long)(q.tail[x] - q.head[x]);
-        q.inspected += ef;
-        q.alg_bytes += 12ull * nf + 8ull * ef + 8ull * nnew;
+        q.inspected += k;
+        q.alg_bytes += 12ull * nf + 8ull * k + 8ull * nnew;
     } else {
-        const unsigned long long k = bu_total - q.bu_seen;
         q.inspected += k;
         q.alg_bytes += 12ull * (unsigned long long)q.nv + 8ull * k + 8ull * nnew;
         q.bu_steps++;
@@ -393,7 +394,8 @@ __device__ void run_step(int mode, const GraphPair &gp, int side, int dir, int l
                          int tile_v = T)
 {
     const DGraph &gx = side ? gp.rev : gp.fwd;
-    AppendTarget app{log, cap, side, tail_ctr, deg_ctr, gx.row_ptr, hist};
+    // top-down reads and bottom-up checks add to the same counter
+    AppendTarget app{log, cap, side, tail_ctr, deg_ctr, gx.row_ptr, hist, bu_ins};
     if (dir == DIR_TD) {
         if (mode == MODE_BFS) {
             VisitBFS vis{levels, level + 1};
@@ -423,10 +425,10 @@ __device__ void run_team_jobs(int mode, const GraphPair &gp, int side, int level
                               int njobs, int team_rank, int team_size, uint8_t *status,
                               int32_t *levels, int32_t *log, int cap, int *tail_ctr,
                               unsigned long long *deg_ctr, int *found, SmemTopDown<T> &sm,
-                              unsigned long long *hist = nullptr)
+                              unsigned long long *hist, unsigned long long *reads)
 {
     const DGraph &gx = side ? gp.rev : gp.fwd;
-    AppendTarget app{log, cap, side, tail_ctr, deg_ctr, gx.row_ptr, hist};
+    AppendTarget app{log, cap, side, tail_ctr, deg_ctr, gx.row_ptr, hist, reads};
     if (mode == MODE_BFS) {
         VisitBFS vis{levels, level + 1};
         team_jobs<T>(gx.col, jobs, njobs, team_rank, team_size, vis, app, sm, nullptr);

@@ -54,6 +54,8 @@ struct AppendTarget {
     const int32_t *row_ptr;   // CSR used to expand this side next time
     unsigned long long *hist; // nullable: packed counts of claimed vertices of degree < 8
                               // (low 32 bits) and >= 128 (high 32 bits)
+    unsigned long long *reads; // nullable: adjacency entries actually read (a step
+                               // that stops early reads fewer than its frontier holds)
 };
 
 __device__ __forceinline__ void log_write(const AppendTarget &a, int pos, int v)
@@ -161,6 +163,7 @@ __device__ __forceinline__ void walk_range(const int32_t *__restrict__ col, int 
                                            int lane_idx, int nlanes, const Vis &vis,
                                            const AppendTarget &app)
 {
+    if (app.reads && lane_idx == 0 && e > b) atomicAdd(app.reads, (unsigned long long)(e - b));
     int a = min((b + 3) & ~3, e);
     int z = max(e & ~3, a);
     int nhead = a - b, ntail = e - z;
@@ -289,6 +292,7 @@ __device__ __forceinline__ void expand_lb(const int32_t *__restrict__ col, int r
     sm.rbs[tid] = rb;
     __syncthreads();
     const int total = sm.total;
+    int nread = 0;
     for (int base = 0; base < total; base += T * K) {
         // a set stop flag (the sides met) ends the tile within one round;
         // the test is warp-uniform, the rounds hold no CTA barrier
@@ -299,12 +303,17 @@ __device__ __forceinline__ void expand_lb(const int32_t *__restrict__ col, int r
             const int e = base + j * T + tid;
             v[j] = -1;
             if (e < total) {
+                ++nread;
                 const int r = lb_row<T>(sm.off, e);
                 v[j] = __ldg(col + sm.rbs[r] + (e - sm.off[r]));
             }
         }
         visit_k<K>(vis, v, c);
         warp_append<K>(c, app);
+    }
+    if (app.reads) {
+        nread = warp_sum_i(nread);
+        if (lane_id() == 0 && nread) atomicAdd(app.reads, (unsigned long long)nread);
     }
     __syncthreads();  // the next tile rewrites off / rbs
 }
@@ -336,6 +345,7 @@ __device__ __forceinline__ void expand_warp(const int32_t *__restrict__ col, int
     const int incl = warp_inclusive_scan(d);
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     const int excl = incl - d;
+    if (app.reads && lane == 0 && total > 0) atomicAdd(app.reads, (unsigned long long)total);
     for (int base = 0; base < total; base += 32) {
         const int e = base + lane;
         int pos = 0;  // number of lanes whose rows end at or before edge e
@@ -377,6 +387,10 @@ __device__ __forceinline__ void expand_thread(const int32_t *__restrict__ col, i
     int mx = len;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (app.reads) {
+        const int sum = warp_sum_i(len);
+        if (lane == 0 && sum > 0) atomicAdd(app.reads, (unsigned long long)sum);
+    }
     for (int k = 0; k < mx; ++k) {
         int c[1] = {-1};
         if (k < len) c[0] = vis.visit(__ldg(col + rb + k));

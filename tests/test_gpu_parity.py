@@ -475,3 +475,23 @@ def test_autotune_batch(fastcon_lib, oracle_mod):
     assert o.tile_entries in (4096, 8192, 16384)
     conn, hops = fc.stcon_batch(G, s, t, opts=o)
     assert (hops == want).all()
+
+
+# --------------------------------------------------------------------------
+# the statistics count adjacency entries actually read: a plain top-down BFS
+# expands every reached vertex once, so it reads exactly their degree sum
+# --------------------------------------------------------------------------
+def test_entries_read_accounting(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    u, v = graphs.rmat_edges(15, 8 << 15, seed=111, perm_seed=112)
+    G = fc.Graph.from_edges(u, v, 1 << 15)
+    rp, col = oracle_mod.build_csr(1 << 15, u, v)
+    deg = np.diff(rp)
+    for src in (0, 77, 4096):
+        lev, _ = oracle_mod.bfs_levels(rp, col, src)
+        want = int(deg[lev >= 0].sum())
+        for eng in ("hostloop", "persistent", "batched"):
+            o = opts(fc, eng, "plain")
+            got, st = G.bfs_levels(src, o, stats=True)
+            assert (got == lev).all()
+            assert st["edges_inspected"] == want, (eng, src, st["edges_inspected"], want)
