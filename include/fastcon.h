@@ -93,7 +93,9 @@ typedef struct fc_stats {
     double  gpu_ms;           /* device time of the call (CUDA events)       */
     int64_t alg_bytes;        /* algorithmic HBM bytes of all steps: 4-byte
                                  status words, 8 per row range, 4 per column
-                                 and queue entry (top-down 12|F| + 8E_F + 8|N|;
+                                 and queue entry (top-down 12|F| + 8E_F + 8|N|,
+                                 E_F the entries the step read: a meeting step
+                                 that stops early counts only what it read;
                                  bottom-up 12 per scanned vertex + 8 per
                                  neighbour checked + 8|N|)                    */
     int32_t escalated;        /* batched: queries finished by the grid engine */
