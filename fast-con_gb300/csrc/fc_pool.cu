@@ -38,6 +38,9 @@ namespace fc {
 constexpr int POOL_TILE_V = 8192;    // vertices per bottom-up tile
 constexpr int POOL_TILE_R = 8192;    // log entries per reset tile
 constexpr int POOL_JOBS = 16384;     // row jobs per slot and step
+// An owner waiting for the helpers of its published step takes other slots'
+// tiles meanwhile (throughput) or only waits (its own query's latency).
+constexpr bool OWNER_HELPS = true;
 constexpr unsigned long long PK_MASK = (1ull << 22) - 1;
 constexpr unsigned long long POOL_IDLE_NS = 4000000000ull;  // 4 s without progress
 
@@ -365,7 +368,7 @@ __device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const Pool
         }
         __syncthreads();
     }
-    // wait for helpers, helping others meanwhile
+    // wait for helpers (helping others meanwhile when OWNER_HELPS)
     if (tid == 0) sm.t_idle = global_timer_ns();
     while (true) {
         if (tid == 0) {
@@ -380,7 +383,7 @@ __device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const Pool
         }
         __syncthreads();
         if (sm.flag) break;
-        if (pool_steal<T>(a, sm)) {
+        if (OWNER_HELPS && pool_steal<T>(a, sm)) {
             if (tid == 0) sm.t_idle = global_timer_ns();
         } else if (tid == 0) {
             __nanosleep(128);
