@@ -324,6 +324,24 @@ __device__ bool pool_steal(const PoolArgs &a, SmemPool<T> &sm)
     return true;
 }
 
+// Once the two sides have met, the step's unclaimed tiles need not run: move
+// the tile counter to ntiles and count them done, so the owner waits only for
+// tiles already in flight.  A row job pushed later by such a tile raises
+// ntiles again and is cancelled on the owner's next look.  Bounded retries.
+__device__ __forceinline__ void cancel_unclaimed(PoolSlot *my)
+{
+    unsigned long long v = ld_acquire_u64(&my->next);
+    for (int it = 0; it < 64 && pk_tile(v) < pk_ntiles(v); ++it) {
+        const unsigned long long n = (unsigned long long)pk_ntiles(v);
+        const unsigned long long old = atomicCAS(&my->next, v, (v & ~PK_MASK) | n);
+        if (old == v) {
+            atomicAdd(&my->done, (int)(n - (unsigned long long)pk_tile(v)));
+            return;
+        }
+        v = old;
+    }
+}
+
 // Publish a step of my slot, run its tiles, help others until it completes.
 template <int T>
 __device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const PoolDesc &desc,
@@ -346,6 +364,8 @@ __device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const Pool
     while (true) {
         if (tid == 0) {
             sm.claimed = -1;
+            if (desc.mode == MODE_STCON && desc.dir != DIR_RESET && ld_cg(&my->tc.found))
+                cancel_unclaimed(my);
             unsigned long long v = ld_acquire_u64(&my->next);
             while (pk_tile(v) < pk_ntiles(v)) {
                 unsigned long long w = atomicCAS(&my->next, v, v + 1);
@@ -372,6 +392,8 @@ __device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const Pool
     if (tid == 0) sm.t_idle = global_timer_ns();
     while (true) {
         if (tid == 0) {
+            if (desc.mode == MODE_STCON && desc.dir != DIR_RESET && ld_cg(&my->tc.found))
+                cancel_unclaimed(my);
             int dn = ld_acquire_gpu(&my->done);
             unsigned long long v = ld_acquire_u64(&my->next);
             sm.flag = dn >= pk_ntiles(v) ? 1 : 0;
