@@ -100,13 +100,15 @@ struct SlotSink {
         int n = (e - b + split - 1) / split;
         int k = atomicAdd(&slot->njobs, n);
         if (k + n > POOL_JOBS) return false;  // job space exhausted: walk in place
+        // every descriptor, one fence, then the seq stamps a claimer waits
+        // for (a fence per job serialised hub rows of ~50 jobs)
         for (int i = 0; i < n; ++i) {
             RowJob &J = jobs[k + i];
             J.b = b + i * split;
             J.e = min(e, J.b + split);
-            __threadfence();
-            *(volatile unsigned *)&J.seq = seq;
         }
+        __threadfence();
+        for (int i = 0; i < n; ++i) *(volatile unsigned *)&jobs[k + i].seq = seq;
         __threadfence();
         atomicAdd(&slot->next, (unsigned long long)n << 22);
         return true;
