@@ -25,7 +25,6 @@
 namespace fc {
 
 constexpr int GATHER_PER_THREAD = 8;  // load-balanced search: entries per thread per round
-constexpr int LB_ROWS = 4;            // rows per thread of a CTA-private tile
 constexpr int GATHER_TEAM = 16;       // the same in team steps (whole-grid levels), where more
                                       // loads in flight pay: plain BFS on R-MAT 24 5.1 -> 4.0 ms
 constexpr long long TEAM_TILE_E = 16384;  // team steps: adjacency entries a tile aims at
@@ -202,8 +201,8 @@ struct SmemTopDown {
     int stop;
     int warp_tot[T / 32];
     int total;
-    int off[T * LB_ROWS];  // load-balanced search: exclusive prefix of the tile's row lengths
-    int rbs[T * LB_ROWS];  // and the rows' first entries
+    int off[T];  // load-balanced search: exclusive prefix of the tile's row lengths
+    int rbs[T];  // and the rows' first entries
 };
 
 // Block-wide inclusive scan of x; *total receives the sum.  All threads call.
@@ -267,40 +266,30 @@ struct TeamSink {
 // dependent rounds and three barriers; no row is walked by one warp or one
 // CTA alone.  Rows longer than the sink's job length go to the sink first.
 // ---------------------------------------------------------------------------
-template <int N>
+template <int T>
 __device__ __forceinline__ int lb_row(const int *off, int e)
 {
-    int lo = 0;  // off[0] = 0 <= e: the last row starting at or before e
+    int lo = 0, hi = T;  // off[0] = 0 <= e: the last row starting at or before e
 #pragma unroll
-    for (int s = N / 2; s > 0; s >>= 1) {
+    for (int s = T / 2; s > 0; s >>= 1) {
         const int mid = lo + s;
-        if (mid < N && off[mid] <= e) lo = mid;
+        if (mid < hi && off[mid] <= e) lo = mid;
     }
     return lo;
 }
 
-// R rows per thread (row r of thread tid is row tid * R + r of the tile).
-template <int T, int R, class Vis, class Sink, int K = GATHER_PER_THREAD>
-__device__ __forceinline__ void expand_lb_rows(const int32_t *__restrict__ col, int (&rb)[R],
-                                               const int (&re)[R], const Vis &vis,
-                                               const AppendTarget &app, SmemTopDown<T> &sm,
-                                               const Sink &sink, const int *stop)
+template <int T, class Vis, class Sink, int K = GATHER_PER_THREAD>
+__device__ __forceinline__ void expand_lb(const int32_t *__restrict__ col, int rb, int re,
+                                          const Vis &vis, const AppendTarget &app,
+                                          SmemTopDown<T> &sm, const Sink &sink,
+                                          const int *stop = nullptr)
 {
-    static_assert(R <= LB_ROWS, "rows per thread");
     const int tid = threadIdx.x;
-    int loc[R], s = 0;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        if (re[r] - rb[r] > 0 && sink.push_row(rb[r], re[r])) rb[r] = re[r];
-        loc[r] = s;
-        s += re[r] - rb[r];
-    }
-    const int incl = block_inclusive_scan<T>(s, sm.warp_tot, &sm.total);
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        sm.off[tid * R + r] = incl - s + loc[r];
-        sm.rbs[tid * R + r] = rb[r];
-    }
+    if (re - rb > 0 && sink.push_row(rb, re)) rb = re;
+    const int d = re - rb;
+    const int incl = block_inclusive_scan<T>(d, sm.warp_tot, &sm.total);
+    sm.off[tid] = incl - d;
+    sm.rbs[tid] = rb;
     __syncthreads();
     const int total = sm.total;
     int nread = 0;
@@ -315,7 +304,7 @@ __device__ __forceinline__ void expand_lb_rows(const int32_t *__restrict__ col, 
             v[j] = -1;
             if (e < total) {
                 ++nread;
-                const int r = lb_row<T * R>(sm.off, e);
+                const int r = lb_row<T>(sm.off, e);
                 v[j] = __ldg(col + sm.rbs[r] + (e - sm.off[r]));
             }
         }
@@ -327,18 +316,6 @@ __device__ __forceinline__ void expand_lb_rows(const int32_t *__restrict__ col, 
         if (lane_id() == 0 && nread) atomicAdd(app.reads, (unsigned long long)nread);
     }
     __syncthreads();  // the next tile rewrites off / rbs
-}
-
-// One row per thread.
-template <int T, class Vis, class Sink, int K = GATHER_PER_THREAD>
-__device__ __forceinline__ void expand_lb(const int32_t *__restrict__ col, int rb, int re,
-                                          const Vis &vis, const AppendTarget &app,
-                                          SmemTopDown<T> &sm, const Sink &sink,
-                                          const int *stop = nullptr)
-{
-    int b[1] = {rb};
-    const int e[1] = {re};
-    expand_lb_rows<T, 1, Vis, Sink, K>(col, b, e, vis, app, sm, sink, stop);
 }
 
 // ---------------------------------------------------------------------------
@@ -479,31 +456,6 @@ __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t 
             return;
         }
     }
-    if (team_size == 1) {
-        // one CTA: tiles of LB_ROWS * T vertices, LB_ROWS rows per thread,
-        // so a low-degree frontier pays the tile's fixed costs (row-range
-        // loads, scan, barriers) once per LB_ROWS * T vertices
-        for (int base = 0; base < F; base += LB_ROWS * T) {
-            int rb[LB_ROWS], re[LB_ROWS];
-#pragma unroll
-            for (int r = 0; r < LB_ROWS; ++r) {
-                const int i = base + r * T + tid;
-                rb[r] = re[r] = 0;
-                if (i < F) {
-                    const int u = ld_cg(frontier + i);
-                    rb[r] = __ldg(row_ptr + u);
-                    re[r] = __ldg(row_ptr + u + 1);
-                }
-            }
-            expand_lb_rows<T, LB_ROWS>(col, rb, re, vis, app, sm, sink, stop_flag);
-            if (stop_flag && base + LB_ROWS * T < F) {
-                if (tid == 0) sm.stop = *(volatile const int *)stop_flag;
-                __syncthreads();
-                if (sm.stop) break;
-            }
-        }
-        return;
-    }
     // tiles of tile_v (<= T) frontier vertices, one per thread, dealt
     // round-robin: frontiers of high degree get tiles of fewer vertices
     const long long step = (long long)team_size * tile_v;
@@ -515,7 +467,10 @@ __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t 
             rb = __ldg(row_ptr + u);
             re = __ldg(row_ptr + u + 1);
         }
-        expand_lb<T, Vis, Sink, GATHER_TEAM>(col, rb, re, vis, app, sm, sink, stop_flag);
+        if (team_size > 1)
+            expand_lb<T, Vis, Sink, GATHER_TEAM>(col, rb, re, vis, app, sm, sink, stop_flag);
+        else
+            expand_lb<T>(col, rb, re, vis, app, sm, sink, stop_flag);
         // the stop flag matters only when another tile of this CTA follows
         if (stop_flag && base + step < F) {
             if (tid == 0) sm.stop = *(volatile const int *)stop_flag;
