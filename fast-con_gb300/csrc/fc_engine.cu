@@ -107,7 +107,7 @@ struct PersistArgs {
 };
 
 template <int T>
-__global__ void __launch_bounds__(T) k_persistent(PersistArgs a)
+__global__ void __launch_bounds__(T, 768 / T) k_persistent(PersistArgs a)
 {
     __shared__ SmemTopDown<T> sm;
     __shared__ QLocal ql;

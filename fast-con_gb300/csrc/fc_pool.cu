@@ -575,7 +575,8 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
                     r[2] = x;
                     r[3] = dir0;
                     r[4] = var0;
-                    r[5] = sm.ql.connected && sm.ql.done;
+                    // bit 0: the sides met; bit 1: the step was shared as tiles
+                    r[5] = (sm.ql.connected && sm.ql.done ? 1 : 0) | (sm.publish ? 2 : 0);
                     r[6] = (int32_t)(cost & 0xFFFFFFFFull);
                     r[7] = (int32_t)(cost >> 32);
                     r[8] = (int32_t)(dt & 0xFFFFFFFFull);

@@ -106,52 +106,95 @@ __device__ __forceinline__ void warp_append(const int (&c)[K], const AppendTarge
 }
 
 // ---------------------------------------------------------------------------
-// Visitors: what happens at one neighbour v of a frontier vertex, in two
-// phases so that a thread can have several neighbours' loads in flight:
-// probe(v) reads v's state; settle(v, probed) claims v when it was free and
-// returns v when this thread claimed it, else -1.  visit() = both.
+// Visitors: what happens at one neighbour v of a frontier vertex, in three
+// phases so that a thread has several neighbours' loads AND claims in flight:
+// probe(v) reads v's state; attempt(v, p) issues the claim when v looked free
+// (its result is not examined yet); resolve(v, p, r) returns v when this
+// thread claimed it, else -1, retrying the rare claim that lost only to a
+// neighbouring byte of the same word.  visit() = all three.
 // ---------------------------------------------------------------------------
 struct VisitSTCON {
     uint8_t *status;
     uint8_t next_code;  // st_code(side, level + 1)
     int side;
     int *found;
-    __device__ __forceinline__ int probe(int v) const { return ld_cg_u8(status + v); }
-    __device__ __forceinline__ int settle(int v, int probed) const
+    __device__ __forceinline__ unsigned *word(int v) const
     {
-        uint8_t s = (uint8_t)probed;
+        return reinterpret_cast<unsigned *>(status + (v & ~3));
+    }
+    __device__ __forceinline__ static uint8_t byte_of(unsigned w, int v)
+    {
+        return (uint8_t)(w >> ((unsigned)(v & 3) * 8u));
+    }
+    // the whole status word: a claim compares and swaps all of it
+    __device__ __forceinline__ int probe(int v) const { return (int)__ldcg(word(v)); }
+    __device__ __forceinline__ int attempt(int v, int p) const
+    {
+        const unsigned w = (unsigned)p;
+        if (byte_of(w, v) != ST_UNVISITED) return p;
+        const unsigned sh = (unsigned)(v & 3) * 8u;
+        return (int)atomicCAS(word(v), w, (w & ~(0xFFu << sh)) | ((unsigned)next_code << sh));
+    }
+    __device__ __forceinline__ int resolve(int v, int p, int r) const
+    {
+        uint8_t s = byte_of((unsigned)p, v);
         if (s == ST_UNVISITED) {
-            s = claim_u8(status, v, next_code);
+            if (r == p) return v;  // the CAS saw the word we probed: claimed
+            s = claim_u8_from(status, v, next_code, (unsigned)r);
             if (s == ST_UNVISITED) return v;
         }
         if ((int)(s >> 7) != side) *(volatile int *)found = 1;
         return -1;
     }
-    __device__ __forceinline__ int visit(int v) const { return settle(v, probe(v)); }
+    __device__ __forceinline__ int visit(int v) const
+    {
+        const int p = probe(v);
+        return resolve(v, p, attempt(v, p));
+    }
 };
 
 struct VisitBFS {
     int32_t *levels;
     int32_t next_level;
     __device__ __forceinline__ int probe(int v) const { return ld_cg(levels + v); }
-    __device__ __forceinline__ int settle(int v, int probed) const
+    __device__ __forceinline__ int attempt(int v, int p) const
     {
-        if (probed >= 0) return -1;
-        return atomicCAS(levels + v, -1, next_level) == -1 ? v : -1;
+        return p >= 0 ? p : atomicCAS(levels + v, -1, next_level);
     }
-    __device__ __forceinline__ int visit(int v) const { return settle(v, probe(v)); }
+    __device__ __forceinline__ int resolve(int v, int p, int r) const
+    {
+        return p < 0 && r == -1 ? v : -1;
+    }
+    __device__ __forceinline__ int visit(int v) const
+    {
+        const int p = probe(v);
+        return resolve(v, p, attempt(v, p));
+    }
 };
 
-// K neighbours at once: all K probes are issued before the first claim.
+// K neighbours at once: all K probes are issued before the first claim, and
+// the claims in groups of CLAIM_GROUP, each group's before the first of its
+// results is examined (the group bounds the registers held by results).
 // v[k] < 0 marks an empty entry (c[k] = -1).
+constexpr int CLAIM_GROUP = 2;
+
 template <int K, class Vis>
 __device__ __forceinline__ void visit_k(const Vis &vis, const int (&v)[K], int (&c)[K])
 {
+    constexpr int G = K < CLAIM_GROUP ? K : CLAIM_GROUP;
+    static_assert(K % G == 0, "K must be a multiple of the claim group");
     int p[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) p[k] = v[k] >= 0 ? vis.probe(v[k]) : 0;
 #pragma unroll
-    for (int k = 0; k < K; ++k) c[k] = v[k] >= 0 ? vis.settle(v[k], p[k]) : -1;
+    for (int g = 0; g < K; g += G) {
+        int r[G];
+#pragma unroll
+        for (int k = 0; k < G; ++k) r[k] = v[g + k] >= 0 ? vis.attempt(v[g + k], p[g + k]) : 0;
+#pragma unroll
+        for (int k = 0; k < G; ++k)
+            c[g + k] = v[g + k] >= 0 ? vis.resolve(v[g + k], p[g + k], r[k]) : -1;
+    }
 }
 
 // ---------------------------------------------------------------------------

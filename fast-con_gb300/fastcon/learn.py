@@ -153,7 +153,7 @@ def decode(recs: np.ndarray):
         r = r[np.sort(len(r) - 1 - last)]
     return {
         "q": r[:, 0], "step": r[:, 1], "side": r[:, 2], "dir": r[:, 3], "variant": r[:, 4],
-        "met": r[:, 5],
+        "met": r[:, 5] & 1, "shared": (r[:, 5] >> 1) & 1,
         "cost": r[:, 6].astype(np.uint32).astype(np.int64) + (r[:, 7].astype(np.int64) << 32),
         "ns": r[:, 8].astype(np.uint32).astype(np.int64) + (r[:, 9].astype(np.int64) << 32),
         "claimed": r[:, 10], "frontier": r[:, 11],
