@@ -15,7 +15,11 @@
 // length become row jobs that the whole team shares.  Long rows in the other
 // variants are walked with 16-byte int4 loads of the column array.  Newly
 // claimed vertices are appended to the log with a warp ballot/shuffle scan
-// and one atomicAdd per warp.
+// and one atomicAdd per warp; the load-balanced search first gathers them in
+// a per-warp buffer in shared memory and reserves log space once per
+// WARP_LOG claims (or at the end of the tile), so that a level whose
+// neighbours are mostly visited already does not send one returning atomic
+// per warp and round to the same counter.
 #pragma once
 
 #include <climits>
@@ -56,7 +60,11 @@ struct AppendTarget {
                               // (low 32 bits) and >= 128 (high 32 bits)
     unsigned long long *reads; // nullable: adjacency entries actually read (a step
                                // that stops early reads fewer than its frontier holds)
+    int *wlog = nullptr;  // nullable (shared memory): per-warp claim buffers of
+                          // WARP_LOG entries, warp w's at wlog + w * WARP_LOG
+    int *wcnt = nullptr;  // their fill counts, one per warp
 };
+constexpr int WARP_LOG = 128;
 
 __device__ __forceinline__ void log_write(const AppendTarget &a, int pos, int v)
 {
@@ -64,6 +72,47 @@ __device__ __forceinline__ void log_write(const AppendTarget &a, int pos, int v)
         a.log[pos] = v;
     else
         a.log[a.nv - 1 - pos] = v;
+}
+
+// Move the warp's buffered claims to the log: one reservation on the tail
+// counter; the claimed vertices' degrees are summed for the schedule.  All 32
+// lanes call it; the buffer is empty afterwards.
+__device__ __forceinline__ void warp_flush(const AppendTarget &a)
+{
+    const int w = (int)(threadIdx.x >> 5), lane = (int)lane_id();
+    const int n = a.wcnt[w];
+    if (n == 0) return;
+    const int *buf = a.wlog + w * WARP_LOG;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(a.tail, n);
+    int v[WARP_LOG / 32], d[WARP_LOG / 32];
+#pragma unroll
+    for (int j = 0; j < WARP_LOG / 32; ++j) {
+        const int i = j * 32 + lane;
+        v[j] = i < n ? buf[i] : -1;
+        d[j] = v[j] >= 0 ? __ldg(a.row_ptr + v[j] + 1) - __ldg(a.row_ptr + v[j]) : 0;
+    }
+    base = __shfl_sync(0xffffffffu, base, 0);
+    long long dsum = 0;
+    int h0 = 0, h2 = 0;
+#pragma unroll
+    for (int j = 0; j < WARP_LOG / 32; ++j)
+        if (v[j] >= 0) {
+            log_write(a, base + j * 32 + lane, v[j]);
+            dsum += d[j];
+            h0 += d[j] < 8;
+            h2 += d[j] >= 128;
+        }
+    dsum = warp_sum_ll(dsum);
+    if (lane == 0) atomicAdd(a.deg, (unsigned long long)dsum);
+    if (a.hist) {
+        const unsigned long long hw =
+            (unsigned long long)warp_sum_i(h0) | ((unsigned long long)warp_sum_i(h2) << 32);
+        if (lane == 0 && hw) atomicAdd(a.hist, hw);
+    }
+    __syncwarp();
+    if (lane == 0) a.wcnt[w] = 0;
+    __syncwarp();
 }
 
 // All 32 lanes of the warp must call this with the same K.
@@ -77,6 +126,23 @@ __device__ __forceinline__ void warp_append(const int (&c)[K], const AppendTarge
     if (!any) return;
     int incl = warp_inclusive_scan(cnt);
     int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (a.wlog && total <= WARP_LOG) {
+        const int w = (int)(threadIdx.x >> 5);
+        int n0 = a.wcnt[w];
+        if (n0 + total > WARP_LOG) {
+            warp_flush(a);
+            n0 = 0;
+        }
+        int *buf = a.wlog + w * WARP_LOG;
+        int pos = n0 + incl - cnt;
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (c[k] >= 0) buf[pos++] = c[k];
+        __syncwarp();
+        if (lane_id() == 0) a.wcnt[w] = n0 + total;
+        __syncwarp();
+        return;
+    }
     long long dsum = 0;
     int h0 = 0, h2 = 0;
 #pragma unroll
@@ -246,6 +312,8 @@ struct SmemTopDown {
     int total;
     int off[T];  // load-balanced search: exclusive prefix of the tile's row lengths
     int rbs[T];  // and the rows' first entries
+    int wcnt[T / 32];           // per-warp claim buffers (AppendTarget::wlog)
+    int wlog[T / 32][WARP_LOG];
 };
 
 // Block-wide inclusive scan of x; *total receives the sum.  All threads call.
@@ -336,6 +404,11 @@ __device__ __forceinline__ void expand_lb(const int32_t *__restrict__ col, int r
     __syncthreads();
     const int total = sm.total;
     int nread = 0;
+    AppendTarget bapp = app;  // claims gathered per warp, flushed below
+    bapp.wlog = &sm.wlog[0][0];
+    bapp.wcnt = sm.wcnt;
+    if (lane_id() == 0) sm.wcnt[tid >> 5] = 0;
+    __syncwarp();
     for (int base = 0; base < total; base += T * K) {
         // a set stop flag (the sides met) ends the tile within one round;
         // the test is warp-uniform, the rounds hold no CTA barrier
@@ -352,8 +425,9 @@ __device__ __forceinline__ void expand_lb(const int32_t *__restrict__ col, int r
             }
         }
         visit_k<K>(vis, v, c);
-        warp_append<K>(c, app);
+        warp_append<K>(c, bapp);
     }
+    warp_flush(bapp);
     if (app.reads) {
         nread = warp_sum_i(nread);
         if (lane_id() == 0 && nread) atomicAdd(app.reads, (unsigned long long)nread);
