@@ -2,6 +2,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fastcon|reference]
                     [--config rmat24|rmat22|er65536|grid4096|batched512] [--sched heuristic|plain|learned]
+    python bench.py --bfs plain|heuristic [--engine hostloop|persistent] [--config ...]
 
 Default workload (rmat24): R-MAT scale 24 (16,777,216 vertices; 8 * 2^24 edge
 samples with a/b/c/d = .57/.19/.19/.05 -> average degree ~16 after
@@ -513,6 +514,35 @@ def run_fastcon(args, cfg):
         dist.destroy_process_group()
 
 
+def run_bfs(args, cfg):
+    """One full BFS of the workload's (first) graph from the vertex at three
+    quarters of the degree order (a hub-connected source), --warmup untimed and
+    --steps timed calls; prints level sizes and the fastest call's device time.
+    The small case that the per-level ncu summaries profile."""
+    import torch
+    torch.cuda.set_device(0)
+    import fastcon as fc
+    Gs, _, _, _ = make_workload_gpu(fc, cfg)
+    G = Gs[0]
+    rp, _ = G.csr_row_ptr()
+    deg = np.diff(rp)
+    src = int(np.argsort(deg)[len(deg) // 2 + len(deg) // 4])
+    o = fc.make_opts(sched=fc.SCHED_PLAIN if args.bfs == "plain" else fc.SCHED_HEURISTIC,
+                     engine=fc.ENGINE_HOSTLOOP if args.engine == "hostloop"
+                     else fc.ENGINE_PERSISTENT)
+    ms = []
+    for k in range(args.warmup + args.steps):
+        lev, st = G.bfs_levels(src, o, stats=True)
+        if k >= args.warmup:
+            ms.append(st["gpu_ms"])
+    reached = lev >= 0
+    entries = int(deg[reached].sum())
+    print(json.dumps({"bfs": args.bfs, "engine": args.engine, "workload": args.config,
+                      "source": src, "levels": np.bincount(lev[reached]).tolist(),
+                      "ms": min(ms), "entries_inspected": int(st["edges_inspected"]),
+                      "gteps_entries": entries / (min(ms) * 1e6)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -521,6 +551,10 @@ def main():
     ap.add_argument("--impl", default="fastcon", choices=["fastcon", "reference"])
     ap.add_argument("--config", default="rmat24", choices=sorted(CONFIGS))
     ap.add_argument("--sched", default="learned", choices=["heuristic", "plain", "learned"])
+    ap.add_argument("--bfs", default=None, choices=["plain", "heuristic"],
+                    help="time one full BFS of the workload's graph instead of the batch")
+    ap.add_argument("--engine", default="hostloop", choices=["hostloop", "persistent"],
+                    help="engine of --bfs")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     import oracle
@@ -534,7 +568,10 @@ def main():
         mod = importlib.util.module_from_spec(spec)
         spec.loader.exec_module(mod)
         mod.build()
-        run_fastcon(args, cfg)
+        if args.bfs:
+            run_bfs(args, cfg)
+        else:
+            run_fastcon(args, cfg)
 
 
 if __name__ == "__main__":
