@@ -131,6 +131,7 @@ struct SmemPool {
     // atomics and reads instead of global ones on every step's critical
     // path; copied to the slot before a published step and back after it
     TeamCounters stc;
+    float mlp[MLP_STORE];  // the learned schedule's weights and box, staged per launch
 };
 
 // counters the helpers of a published step add to
@@ -476,9 +477,9 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             if (a.trace || consult) {
                 float f[MLP_IN];
                 ql_features(sm.ql, f);
-                if (consult && mlp_in_box(a.mlp, f)) {
+                if (consult && mlp_in_box(sm.mlp, f)) {
                     float o[MLP_OUT];
-                    mlp_forward_warp(a.mlp, f, o);
+                    mlp_forward_warp(sm.mlp, f, o);
                     if (tid == 0) {
                         ql_apply_logits(sm.ql, o, 1, bu_cap);
                         if (a.force_variant >= 0) sm.ql.variant = a.force_variant;
@@ -635,6 +636,8 @@ __global__ void __launch_bounds__(T, 768 / T) k_pool(PoolArgs a)
         // continue this slot's seq numbering across launches
         sm.my_seq = pk_seq(__ldcg(&my->next));
     }
+    if (a.sched == FC_SCHED_LEARNED && a.mlp)
+        for (int i = tid; i < MLP_STORE; i += T) sm.mlp[i] = __ldg(a.mlp + i);
     __syncthreads();
     if (!a.exclusive || blockIdx.x == 0) {
         uint8_t *status = a.status_base + (a.exclusive ? 0 : (size_t)blockIdx.x * a.status_stride);

@@ -284,25 +284,26 @@ __host__ __device__ inline void mlp_forward_scalar(const float *W, const float *
 }
 
 // Forward pass by one warp: lane j computes hidden unit j of both layers; the
-// 7 outputs are warp reductions.  Every lane returns all 7 logits.
-__device__ __forceinline__ void mlp_forward_warp(const float *__restrict__ W, const float *f,
-                                                 float *out)
+// 7 outputs are warp reductions.  Every lane returns all 7 logits.  W is the
+// CTA's shared-memory copy of the weights (the batched engine stages them
+// once per launch), so no step waits on an L2 round trip for them.
+__device__ __forceinline__ void mlp_forward_warp(const float *W, const float *f, float *out)
 {
     const int j = (int)lane_id();
-    float a = __ldg(W + MLP_B1 + j);
+    float a = W[MLP_B1 + j];
 #pragma unroll
-    for (int i = 0; i < MLP_IN; ++i) a += __ldg(W + MLP_W1 + j * MLP_IN + i) * f[i];
+    for (int i = 0; i < MLP_IN; ++i) a += W[MLP_W1 + j * MLP_IN + i] * f[i];
     const float h1 = a > 0.f ? a : 0.f;
-    a = __ldg(W + MLP_B2 + j);
+    a = W[MLP_B2 + j];
 #pragma unroll 8
-    for (int k = 0; k < MLP_H; ++k) a += __ldg(W + MLP_W2 + j * MLP_H + k) * __shfl_sync(0xffffffffu, h1, k);
+    for (int k = 0; k < MLP_H; ++k) a += W[MLP_W2 + j * MLP_H + k] * __shfl_sync(0xffffffffu, h1, k);
     const float h2 = a > 0.f ? a : 0.f;
 #pragma unroll
     for (int o = 0; o < MLP_OUT; ++o) {
-        float v = __ldg(W + MLP_W3 + o * MLP_H + j) * h2;
+        float v = W[MLP_W3 + o * MLP_H + j] * h2;
 #pragma unroll
         for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-        out[o] = v + __ldg(W + MLP_B3 + o);
+        out[o] = v + W[MLP_B3 + o];
     }
 }
 
