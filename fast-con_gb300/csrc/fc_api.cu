@@ -691,15 +691,18 @@ int fc_stcon_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *graph_id
     std::vector<fc::GraphPairH> pairs((size_t)ngraphs);
     for (int i = 0; i < ngraphs; ++i) pairs[(size_t)i] = pair_of(gs[i]);
     fc_opts o = opts ? *opts : default_opts();
+    // the answers' copies and the engine's error words travel together, so
+    // the call waits once
     rc = fc::engine_stcon_batch(L.c, pairs.data(), ngraphs, graph_idx ? dg : nullptr, ds, dt, nq,
-                                dc, dh, o, stats, st, true);
+                                dc, dh, o, stats, st, fc::BATCH_DEFER_CHECK);
     if (rc == FC_OK) {
         FC_CUDA_TRY(cudaMemcpyAsync(connected, dc, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, st));
         FC_CUDA_TRY(cudaMemcpyAsync(hops, dh, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, st));
     }
     // the staging buffer is reused by the next call
     cudaStreamSynchronize(st);
-    return rc;
+    const int crc = fc::engine_finish_checks(L.c);
+    return rc != FC_OK ? rc : crc;
 }
 
 }  // extern "C"

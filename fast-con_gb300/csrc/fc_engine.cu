@@ -258,7 +258,8 @@ DevCtx *get_ctx(int *err)
             cudaEventCreate(&c->evm) != cudaSuccess ||
             cudaMalloc(&c->tc, sizeof(TeamCounters)) != cudaSuccess ||
             cudaMallocHost(&c->h_tc, sizeof(TeamCounters)) != cudaSuccess ||
-            cudaMalloc(&c->b_ctr, 8 * sizeof(int)) != cudaSuccess) {
+            cudaMalloc(&c->b_ctr, 8 * sizeof(int)) != cudaSuccess ||
+            cudaMallocHost(&c->h_bctr, 8 * sizeof(int)) != cudaSuccess) {
             *err = FC_ERR_CUDA;
             set_error("device context set-up failed");
             return nullptr;
@@ -346,10 +347,9 @@ static int launch_persistent(DevCtx *c, const PersistArgs &a, cudaStream_t st)
     return FC_OK;
 }
 
-static int check_counters(DevCtx *c, cudaStream_t st)
+// After the copy of tc to h_tc has completed.
+static int counters_verdict(DevCtx *c)
 {
-    FC_CUDA_TRY(cudaMemcpyAsync(c->h_tc, c->tc, sizeof(TeamCounters), cudaMemcpyDeviceToHost, st));
-    FC_CUDA_TRY(cudaStreamSynchronize(st));
     if (c->h_tc->err) {
         set_error("device-side wait timed out (bounded grid barrier)");
         // leave the workspace clean for the next call
@@ -359,6 +359,13 @@ static int check_counters(DevCtx *c, cudaStream_t st)
         return FC_ERR_TIMEOUT;
     }
     return FC_OK;
+}
+
+static int check_counters(DevCtx *c, cudaStream_t st)
+{
+    FC_CUDA_TRY(cudaMemcpyAsync(c->h_tc, c->tc, sizeof(TeamCounters), cudaMemcpyDeviceToHost, st));
+    FC_CUDA_TRY(cudaStreamSynchronize(st));
+    return counters_verdict(c);
 }
 
 // Host-loop engine: one launch per step; returns the final QLocal.
@@ -544,11 +551,10 @@ static int ensure_pool(DevCtx *c)
     return FC_OK;
 }
 
-static int check_pool(DevCtx *c, cudaStream_t st, int *invalid)
+// After the copy of b_ctr to h_bctr has completed.
+static int pool_verdict(DevCtx *c, int *invalid)
 {
-    int h[8];
-    FC_CUDA_TRY(cudaMemcpyAsync(h, c->b_ctr, sizeof(h), cudaMemcpyDeviceToHost, st));
-    FC_CUDA_TRY(cudaStreamSynchronize(st));
+    const int *h = c->h_bctr;
     if (invalid) *invalid = h[4];
     if (h[3]) {
         set_error("device-side wait timed out in the pool engine");
@@ -560,6 +566,25 @@ static int check_pool(DevCtx *c, cudaStream_t st, int *invalid)
         return FC_ERR_TIMEOUT;
     }
     return FC_OK;
+}
+
+static int check_pool(DevCtx *c, cudaStream_t st, int *invalid)
+{
+    FC_CUDA_TRY(cudaMemcpyAsync(c->h_bctr, c->b_ctr, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    FC_CUDA_TRY(cudaStreamSynchronize(st));
+    return pool_verdict(c, invalid);
+}
+
+int engine_finish_checks(DevCtx *c)
+{
+    const int e = c->deferred_engine;
+    c->deferred_engine = -1;
+    if (e < 0) return FC_OK;
+    if (e != FC_ENGINE_PERSISTENT) {
+        const int rc = pool_verdict(c, nullptr);
+        if (rc) return rc;
+    }
+    return counters_verdict(c);
 }
 
 static long long private_edges_default(const fc_opts &o, bool)
@@ -783,9 +808,10 @@ static int ensure_batch_arena(DevCtx *c, size_t slots, size_t maxnv, int log_cap
 int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int32_t *d_gi,
                        const int32_t *d_s, const int32_t *d_t, int32_t nq, int32_t *d_conn,
                        int32_t *d_hops, const fc_opts &o, fc_stats *st, cudaStream_t stream,
-                       bool sync, const BatchExtras *ex)
+                       int check, const BatchExtras *ex)
 {
     constexpr int T = FC_BLOCK;
+    c->deferred_engine = -1;
     if (nq <= 0) return FC_OK;
     if (ex && pick_engine(o, FC_ENGINE_BATCHED) != FC_ENGINE_BATCHED) {
         set_error("scripts and traces need the batched engine");
@@ -1014,7 +1040,16 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         return FC_ERR_UNSUPPORTED;
     }
     FC_CUDA_TRY(cudaEventRecord(c->ev1, stream));
-    if (sync || st) {
+    if (check == BATCH_DEFER_CHECK && !st) {
+        if (engine != FC_ENGINE_PERSISTENT)
+            FC_CUDA_TRY(cudaMemcpyAsync(c->h_bctr, c->b_ctr, 8 * sizeof(int),
+                                        cudaMemcpyDeviceToHost, stream));
+        FC_CUDA_TRY(cudaMemcpyAsync(c->h_tc, c->tc, sizeof(TeamCounters), cudaMemcpyDeviceToHost,
+                                    stream));
+        c->deferred_engine = engine;
+        return FC_OK;
+    }
+    if (check || st) {
         rc = engine == FC_ENGINE_PERSISTENT ? check_counters(c, stream) : check_pool(c, stream, nullptr);
         if (rc) return rc;
         if (engine == FC_ENGINE_BATCHED && (rc = check_counters(c, stream))) return rc;

@@ -67,6 +67,9 @@ struct DevCtx {
     int mlp_ready = 0;
     int b_log_cap = 0;
     int *b_ctr = nullptr;            // [0] next query, [1] spill count, [2] error
+    int *h_bctr = nullptr;           // pinned mirror of b_ctr
+    int deferred_engine = -1;        // engine whose error words are in flight to
+                                     // h_bctr / h_tc (BATCH_DEFER_CHECK), else -1
     int32_t *b_spill = nullptr;
     size_t b_spill_cap = 0;
     QueryStat *qstat = nullptr;
@@ -109,10 +112,20 @@ struct BatchExtras {
     long long *inspected = nullptr;         // per query
 };
 
+// check: BATCH_NO_CHECK returns once the launches are queued; BATCH_CHECK
+// waits for them and reads the device-side error words; BATCH_DEFER_CHECK
+// queues the copies of those words to pinned host memory and returns, and the
+// caller calls engine_finish_checks after its own synchronisation of the
+// stream (one wait for the results and the checks together).  Statistics
+// (st != nullptr) always wait.
+constexpr int BATCH_NO_CHECK = 0, BATCH_CHECK = 1, BATCH_DEFER_CHECK = 2;
 int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int32_t *d_gi,
                        const int32_t *d_s, const int32_t *d_t, int32_t nq, int32_t *d_conn,
                        int32_t *d_hops, const fc_opts &o, fc_stats *st, cudaStream_t stream,
-                       bool sync, const BatchExtras *ex = nullptr);
+                       int check, const BatchExtras *ex = nullptr);
+// The error words a BATCH_DEFER_CHECK call queued, read after the stream was
+// synchronised: FC_OK, or FC_ERR_TIMEOUT with the workspaces reset.
+int engine_finish_checks(DevCtx *c);
 
 // BFS tree, shortest path, predecessor-map validation (fc_tree.cu).
 int engine_bfs_parents(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_parents,

@@ -318,19 +318,31 @@ class Graph:
         return int(d[0])
 
 
-def stcon_batch(graphs, s, t, graph_idx=None, opts: Opts | None = None, stats: bool = False):
-    """Many (s, t) queries over one or several graphs; host arrays in/out."""
+def stcon_batch(graphs, s, t, graph_idx=None, opts: Opts | None = None, stats: bool = False,
+                out=None):
+    """Many (s, t) queries over one or several graphs; host arrays in/out.
+    out: optional (connected, hops) int32 arrays of at least len(s) entries to
+    fill (page-locked ones keep the result copies asynchronous).  Statistics
+    are gathered only when stats is true (they add a copy of per-query
+    counters to the call)."""
     if isinstance(graphs, Graph):
         graphs = [graphs]
     arr = (ctypes.c_void_p * len(graphs))(*[g.handle.value for g in graphs])
     s, t = _i32(s), _i32(t)
     gi = _i32(graph_idx) if graph_idx is not None else None
     nq = len(s)
-    conn = np.zeros(nq, np.int32)
-    hops = np.zeros(nq, np.int32)
-    st = Stats()
+    if out is not None:
+        conn, hops = out
+        for a in (conn, hops):
+            if a.dtype != np.int32 or not a.flags["C_CONTIGUOUS"] or len(a) < nq:
+                raise ValueError("out arrays must be contiguous int32 of at least len(s) entries")
+    else:
+        conn = np.zeros(nq, np.int32)
+        hops = np.zeros(nq, np.int32)
+    st = Stats() if stats else None
     _check(lib().fc_stcon_batch(arr, len(graphs), _P(gi), _P(s), _P(t), nq, _P(conn), _P(hops),
-                                ctypes.byref(opts) if opts else None, ctypes.byref(st)),
+                                ctypes.byref(opts) if opts else None,
+                                ctypes.byref(st) if st is not None else None),
            "fc_stcon_batch")
     return (conn, hops, st.as_dict()) if stats else (conn, hops)
 

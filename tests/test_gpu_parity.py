@@ -145,6 +145,26 @@ def test_batched_graph_replay(fastcon_lib, er_graph, er_golden):
     assert (hops == want).all() and st["graph"] == 0
 
 
+@pytest.mark.parametrize("engine", ENGINES_BATCH)
+def test_batch_into_caller_arrays_without_stats(fastcon_lib, er_graph, er_golden, engine):
+    """Host-array batches without statistics wait once for the answers and the
+    engine's error words together; answers land in the caller's arrays."""
+    import torch
+    fc = fastcon_lib
+    s, t = np.array(er_golden["s"]), np.array(er_golden["t"])
+    want = np.array(er_golden["hops"])
+    hc = torch.full((len(s) + 3,), -7, dtype=torch.int32).pin_memory().numpy()
+    hh = torch.full((len(s) + 3,), -7, dtype=torch.int32).pin_memory().numpy()
+    o = opts(fc, engine, "heuristic")
+    for _ in range(2):  # the second call reuses the staging (and a captured graph)
+        conn, hops = fc.stcon_batch(er_graph, s, t, opts=o, out=(hc, hh))
+        assert conn is hc and hops is hh
+        assert (hh[:len(s)] == want).all() and (hc[:len(s)] == (want >= 0)).all()
+        assert (hh[len(s):] == -7).all()  # nothing written past the batch
+    with pytest.raises(ValueError):
+        fc.stcon_batch(er_graph, s, t, opts=o, out=(hc[:10], hh))
+
+
 # --------------------------------------------------------------------------
 # the reference's known-answer run (Graph500 R-MAT scale 16)
 # --------------------------------------------------------------------------
