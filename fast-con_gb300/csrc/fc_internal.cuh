@@ -120,37 +120,6 @@ __device__ __forceinline__ void st_release_gpu(int *p, int v)
 }
 
 // ---------------------------------------------------------------------------
-// Byte-granular claim on the status array: one 32-bit atomicCAS on the word
-// holding the byte.  Returns the byte value seen: ST_UNVISITED means this
-// thread claimed it.  The loop retries only when a neighbouring byte of the
-// same word changed in between; each byte changes at most once per step, so
-// it ends after at most four attempts.  `old` = the word as last seen (a load
-// or a failed CAS's return value).
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint8_t claim_u8_from(uint8_t *status, int v, uint8_t code,
-                                                 unsigned old)
-{
-    unsigned *w = reinterpret_cast<unsigned *>(status + (v & ~3));
-    unsigned sh = (unsigned)(v & 3) * 8u;
-#pragma unroll 1
-    for (int attempt = 0; attempt < 8; ++attempt) {
-        uint8_t b = (uint8_t)((old >> sh) & 0xFFu);
-        if (b != ST_UNVISITED) return b;
-        unsigned nw = (old & ~(0xFFu << sh)) | ((unsigned)code << sh);
-        unsigned prev = atomicCAS(w, old, nw);
-        if (prev == old) return ST_UNVISITED;
-        old = prev;
-    }
-    return (uint8_t)((old >> sh) & 0xFFu);  // unreachable in practice
-}
-
-__device__ __forceinline__ uint8_t claim_u8(uint8_t *status, int v, uint8_t code)
-{
-    return claim_u8_from(status, v, code,
-                         __ldcg(reinterpret_cast<const unsigned *>(status + (v & ~3))));
-}
-
-// ---------------------------------------------------------------------------
 // Software grid barrier for cooperative launches.  Every wait is bounded by
 // an iteration count and by %globaltimer; on expiry the barrier records
 // FC_ERR_TIMEOUT in *err and returns false, and the caller returns.

@@ -175,9 +175,17 @@ __device__ __forceinline__ void warp_append(const int (&c)[K], const AppendTarge
 // Visitors: what happens at one neighbour v of a frontier vertex, in three
 // phases so that a thread has several neighbours' loads AND claims in flight:
 // probe(v) reads v's state; attempt(v, p) issues the claim when v looked free
-// (its result is not examined yet); resolve(v, p, r) returns v when this
-// thread claimed it, else -1, retrying the rare claim that lost only to a
-// neighbouring byte of the same word.  visit() = all three.
+// and returns the state the claim found (or p); resolve(v, r) returns v when
+// this thread claimed it, else -1.  Only r is kept between attempt and
+// resolve.  visit() = all three.
+//
+// The s-t claim needs no compare: one side expands per step and every claim
+// of a step writes the same code, so an atomicAnd that clears the bits that
+// are 0 in the code turns an unvisited byte (0xFF) into the code and leaves a
+// byte claimed earlier in the step as it was; the byte it returns says which
+// happened.  (A byte of the other side or of an earlier step is never free
+// when probed, so it is never the target of a claim.)  The neighbouring bytes
+// of the word are ANDed with ones and do not change.
 // ---------------------------------------------------------------------------
 struct VisitSTCON {
     uint8_t *status;
@@ -192,31 +200,21 @@ struct VisitSTCON {
     {
         return (uint8_t)(w >> ((unsigned)(v & 3) * 8u));
     }
-    // the whole status word: a claim compares and swaps all of it
     __device__ __forceinline__ int probe(int v) const { return (int)__ldcg(word(v)); }
     __device__ __forceinline__ int attempt(int v, int p) const
     {
-        const unsigned w = (unsigned)p;
-        if (byte_of(w, v) != ST_UNVISITED) return p;
+        if (byte_of((unsigned)p, v) != ST_UNVISITED) return p;
         const unsigned sh = (unsigned)(v & 3) * 8u;
-        return (int)atomicCAS(word(v), w, (w & ~(0xFFu << sh)) | ((unsigned)next_code << sh));
+        return (int)atomicAnd(word(v), ~((0xFFu ^ (unsigned)next_code) << sh));
     }
-    __device__ __forceinline__ int resolve(int v, int p, int r) const
+    __device__ __forceinline__ int resolve(int v, int r) const
     {
-        uint8_t s = byte_of((unsigned)p, v);
-        if (s == ST_UNVISITED) {
-            if (r == p) return v;  // the CAS saw the word we probed: claimed
-            s = claim_u8_from(status, v, next_code, (unsigned)r);
-            if (s == ST_UNVISITED) return v;
-        }
+        const uint8_t s = byte_of((unsigned)r, v);
+        if (s == ST_UNVISITED) return v;
         if ((int)(s >> 7) != side) *(volatile int *)found = 1;
         return -1;
     }
-    __device__ __forceinline__ int visit(int v) const
-    {
-        const int p = probe(v);
-        return resolve(v, p, attempt(v, p));
-    }
+    __device__ __forceinline__ int visit(int v) const { return resolve(v, attempt(v, probe(v))); }
 };
 
 struct VisitBFS {
@@ -227,40 +225,23 @@ struct VisitBFS {
     {
         return p >= 0 ? p : atomicCAS(levels + v, -1, next_level);
     }
-    __device__ __forceinline__ int resolve(int v, int p, int r) const
-    {
-        return p < 0 && r == -1 ? v : -1;
-    }
-    __device__ __forceinline__ int visit(int v) const
-    {
-        const int p = probe(v);
-        return resolve(v, p, attempt(v, p));
-    }
+    __device__ __forceinline__ int resolve(int v, int r) const { return r == -1 ? v : -1; }
+    __device__ __forceinline__ int visit(int v) const { return resolve(v, attempt(v, probe(v))); }
 };
 
 // K neighbours at once: all K probes are issued before the first claim, and
-// the claims in groups of CLAIM_GROUP, each group's before the first of its
-// results is examined (the group bounds the registers held by results).
+// all K claims before the first claim's result is examined.
 // v[k] < 0 marks an empty entry (c[k] = -1).
-constexpr int CLAIM_GROUP = 2;
-
 template <int K, class Vis>
 __device__ __forceinline__ void visit_k(const Vis &vis, const int (&v)[K], int (&c)[K])
 {
-    constexpr int G = K < CLAIM_GROUP ? K : CLAIM_GROUP;
-    static_assert(K % G == 0, "K must be a multiple of the claim group");
-    int p[K];
+    int r[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) p[k] = v[k] >= 0 ? vis.probe(v[k]) : 0;
+    for (int k = 0; k < K; ++k) r[k] = v[k] >= 0 ? vis.probe(v[k]) : 0;
 #pragma unroll
-    for (int g = 0; g < K; g += G) {
-        int r[G];
+    for (int k = 0; k < K; ++k) r[k] = v[k] >= 0 ? vis.attempt(v[k], r[k]) : 0;
 #pragma unroll
-        for (int k = 0; k < G; ++k) r[k] = v[g + k] >= 0 ? vis.attempt(v[g + k], p[g + k]) : 0;
-#pragma unroll
-        for (int k = 0; k < G; ++k)
-            c[g + k] = v[g + k] >= 0 ? vis.resolve(v[g + k], p[g + k], r[k]) : -1;
-    }
+    for (int k = 0; k < K; ++k) c[k] = v[k] >= 0 ? vis.resolve(v[k], r[k]) : -1;
 }
 
 // ---------------------------------------------------------------------------
