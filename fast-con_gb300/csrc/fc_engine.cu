@@ -544,6 +544,8 @@ static int ensure_pool(DevCtx *c)
     }
     FC_CUDA_TRY(cudaMalloc(&c->p_slots, pool_slot_bytes() * (size_t)grid));
     FC_CUDA_TRY(cudaMalloc(&c->p_jobs, pool_job_bytes() * (size_t)grid));
+    FC_CUDA_TRY(cudaMalloc(&c->p_open, sizeof(int) * (size_t)grid));
+    FC_CUDA_TRY(cudaMemset(c->p_open, 0, sizeof(int) * (size_t)grid));
     FC_CUDA_TRY(cudaMemset(c->p_slots, 0, pool_slot_bytes() * (size_t)grid));
     FC_CUDA_TRY(cudaMemset(c->p_jobs, 0, pool_job_bytes() * (size_t)grid));
     FC_CUDA_TRY(cudaDeviceSynchronize());
@@ -560,6 +562,7 @@ static int pool_verdict(DevCtx *c, int *invalid)
         set_error("device-side wait timed out in the pool engine");
         // leave every workspace clean for the next call
         cudaMemset(c->p_slots, 0, pool_slot_bytes() * (size_t)c->p_grid);
+        cudaMemset(c->p_open, 0, sizeof(int) * (size_t)c->p_grid);
         if (c->status) cudaMemset(c->status, 0xFF, (c->ws_nv + 15) / 16 * 16);
         if (c->b_status) cudaMemset(c->b_status, 0xFF, c->b_slots * c->b_status_stride);
         cudaDeviceSynchronize();
@@ -627,6 +630,7 @@ static PoolArgs pool_args_exclusive(DevCtx *c, int mode, const fc_opts &o)
     a.private_variant = -1;
     a.exclusive = 1;
     a.slots = (PoolSlot *)c->p_slots;
+    a.open = c->p_open;
     a.jobs = (RowJob *)c->p_jobs;
     a.status_base = c->status;
     a.levels = c->levels;
@@ -879,6 +883,7 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         a.private_variant = o.private_variant > 0 ? o.private_variant - 1 : -1;
         a.exclusive = 0;
         a.slots = (PoolSlot *)c->p_slots;
+        a.open = c->p_open;
         a.jobs = (RowJob *)c->p_jobs;
         a.status_base = c->b_status;
         a.status_stride = c->b_status_stride;

@@ -59,6 +59,7 @@ struct DevCtx {
     // pool engine: one slot record and one row-job area per resident CTA
     void *p_slots = nullptr;
     void *p_jobs = nullptr;
+    int *p_open = nullptr;           // PoolArgs::open
     int p_grid = 0;
     // learned schedule weights (1,703 floats) and feature box (24 floats),
     // device and host copies

@@ -292,8 +292,11 @@ __device__ bool pool_steal(const PoolArgs &a, SmemPool<T> &sm)
     if (tid == 0) sm.cand = INT_MAX;
     __syncthreads();
     const int cur = sm.cursor;
+    // the open hints are one coalesced read; only open slots' tile words
+    // (one 256-byte record each) are read
     for (int k = tid; k < P; k += T) {
         int j = (cur + k) % P;
+        if (!ld_cg(a.open + j)) continue;
         unsigned long long v = __ldcg(&a.slots[j].next);
         if (pk_tile(v) < pk_ntiles(v)) atomicMin(&sm.cand, k);
     }
@@ -359,6 +362,8 @@ __device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const Pool
         if (sm.my_seq == 0) sm.my_seq = 1;
         __threadfence();
         atomicExch(&my->next, pk(sm.my_seq, (unsigned long long)nvt, 0));
+        __threadfence();
+        *(volatile int *)(a.open + blockIdx.x) = 1;
         sm.d = desc;
     }
     __syncthreads();
@@ -416,6 +421,7 @@ __device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const Pool
         __syncthreads();
     }
     if (tid == 0) {
+        *(volatile int *)(a.open + blockIdx.x) = 0;  // every tile is done
         sm.err = sm.flag == 2;
         sm.d = desc;
     }

@@ -24,6 +24,8 @@ struct PoolArgs {
     int private_variant;      // variant for steps the owner runs alone (-1: the schedule's)
     int exclusive;            // 1: CTA 0 owns every query in turn, arrays span the graph
     PoolSlot *slots;          // one per CTA
+    int *open;                // one per CTA: 1 while its owner has a step published
+                              // (a hint: pollers read only these slots' tile words)
     RowJob *jobs;             // POOL_JOBS per CTA
     uint8_t *status_base;
     size_t status_stride;
