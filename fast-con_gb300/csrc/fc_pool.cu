@@ -396,8 +396,11 @@ __device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const Pool
         }
         __syncthreads();
     }
-    // wait for helpers (helping others meanwhile when OWNER_HELPS)
+    // wait for helpers (helping others meanwhile when OWNER_HELPS); the
+    // launch's error word, set only when some wait timed out, is read every
+    // 16th poll: every waiting CTA reading it each time crowds its L2 line
     if (tid == 0) sm.t_idle = global_timer_ns();
+    unsigned polls = 0;
     while (true) {
         if (tid == 0) {
             if (desc.mode == MODE_STCON && desc.dir != DIR_RESET && ld_cg(&my->tc.found))
@@ -409,7 +412,7 @@ __device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const Pool
                 atomicCAS(&a.ctr[CTR_ERR], 0, FC_ERR_TIMEOUT);
                 sm.flag = 2;
             }
-            if (!sm.flag && ld_cg(&a.ctr[CTR_ERR])) sm.flag = 2;
+            if (!sm.flag && (++polls & 15u) == 0 && ld_cg(&a.ctr[CTR_ERR])) sm.flag = 2;
         }
         __syncthreads();
         if (sm.flag) break;
@@ -668,9 +671,11 @@ __global__ void __launch_bounds__(T, 768 / T) k_pool(PoolArgs a)
         sm.backoff = 128;
     }
     __syncthreads();
+    unsigned polls = 0;
     while (true) {
         if (tid == 0) {
-            sm.flag = ld_acquire_gpu(&a.ctr[CTR_FINISHED]) >= nq || ld_cg(&a.ctr[CTR_ERR]) != 0;
+            sm.flag = ld_acquire_gpu(&a.ctr[CTR_FINISHED]) >= nq ||
+                      ((++polls & 15u) == 0 && ld_cg(&a.ctr[CTR_ERR]) != 0);
             if (!sm.flag && global_timer_ns() - sm.t_idle > POOL_IDLE_NS) {
                 atomicCAS(&a.ctr[CTR_ERR], 0, FC_ERR_TIMEOUT);
                 sm.flag = 1;
