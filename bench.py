@@ -407,8 +407,12 @@ def run_fastcon(args, cfg):
         ratio = json.load(open(tp)).get("k_pool", {}).get("dram_bytes_per_alg_byte")
         if ratio:
             traffic = float(ratio) * float(kbytes[dom])
+    # the same launch in DRAM bytes: scaled traffic over the kernel's time
+    achieved_dram = (traffic / 1e9) / (kms[dom] / 1e3) if traffic and kms[dom] > 0 else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
+                "achieved_dram": achieved_dram,
+                "dram_frac": achieved_dram / peak if achieved_dram else None,
                 "traffic_source": "profiles/traffic_per_unit.json (scaled small-case capture)",
                 "kernel": "k_pool" + (" (shared-work pass)" if dom == 0 else " (exclusive pass)"),
                 "peak_source": f"{peak_src} hbm_gbs (MEASURED_PEAKS.json)",
