@@ -377,8 +377,10 @@ int parse_edgelist_file(const char *path, int relabel, int nthreads, Parsed &P)
                 auto ib = idmap.emplace(C.dst[j], (int32_t)idmap.size()).first;
                 P.dst[k] = ib->second;
             }
-        nv = (long long)idmap.size();
-        maxid = nv - 1;
+        // the header's node count when it is larger (vertices that appear
+        // in no edge), as readGraphHeader sizes the graph from it
+        maxid = (long long)idmap.size() - 1;
+        nv = std::max((long long)idmap.size(), H.declared);
     } else {
         std::vector<size_t> off(ch.size() + 1, 0);
         for (size_t i = 0; i < ch.size(); ++i) off[i + 1] = off[i] + ch[i].src.size();

@@ -544,7 +544,9 @@ int oracle_read_edgelist(const char *path, int relabel, int32_t *nv_out, int64_t
     free(map.vals);
     (void)declared;
     if (bad || fmt == 0) return -1;
-    int64_t nvv = relabel && fmt == 1 ? map.size : nodes;
+    /* renumbered SNAP ids: the header's node count when larger, as
+     * readGraphHeader sizes the graph from it (K/Util/readGraphHeader.cpp:101-114) */
+    int64_t nvv = relabel && fmt == 1 ? (map.size > nodes ? map.size : nodes) : nodes;
     if (nvv < maxid + 1) nvv = maxid + 1;
     if (nvv > INT32_MAX) return -1;
     *nv_out = (int32_t)nvv;

@@ -17,6 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_BFS_PATH = os.path.join(HERE, "_ref", "libref_bfs.so")
 REF_GEN_PATH = os.path.join(HERE, "_ref", "graph500_gen")
+REF_READ_PATH = os.path.join(HERE, "_ref", "libref_read.so")
+REF_LOADGRAPH_PATH = os.path.join(HERE, "_ref", "libref_loadgraph.so")
 
 SYMMETRIZE, DROP_LOOPS, DEDUPE = 1, 2, 4
 CANONICAL = SYMMETRIZE | DROP_LOOPS | DEDUPE
@@ -252,3 +254,49 @@ def ref_bfs_levels(row_ptr, col, sources):
     inf = ref().ref_inf()
     dist[dist == inf] = -1
     return dist, vis
+
+
+# ---------------------------------------------------------------------------
+# The reference's own edge-list readers (compiled from its sources into
+# oracle/_ref/ where the reference tree was available; used only to write the
+# reader fixtures of tests/golden/).
+# ---------------------------------------------------------------------------
+def ref_read_graph(path: str, user_dir: int = 2):
+    """BFS-4K readGraphHeader + readSTD + ToCSR on `path` (user_dir 0
+    directed, 1 undirected, 2 as the file says): dict with V, E, direction
+    (0/1), coo int32[n, 2] in the reader's order, row_ptr, col."""
+    R = ctypes.CDLL(REF_READ_PATH)
+    R.ref_read_graph.restype = ctypes.c_int
+    IP = ctypes.POINTER(ctypes.c_int)
+    R.ref_read_graph.argtypes = [ctypes.c_char_p, ctypes.c_int, IP, IP, IP, IP,
+                                 ctypes.POINTER(IP), ctypes.POINTER(IP), ctypes.POINTER(IP)]
+    R.ref_read_free.argtypes = [ctypes.c_void_p]
+    V, E, d, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    coo, rp, col = IP(), IP(), IP()
+    R.ref_read_graph(path.encode(), int(user_dir), ctypes.byref(V), ctypes.byref(E),
+                     ctypes.byref(d), ctypes.byref(n), ctypes.byref(coo), ctypes.byref(rp),
+                     ctypes.byref(col))
+    out = {"V": V.value, "E": E.value, "direction": d.value,
+           "coo": np.ctypeslib.as_array(coo, shape=(max(1, 2 * n.value),))[: 2 * n.value]
+           .reshape(-1, 2).copy(),
+           "row_ptr": np.ctypeslib.as_array(rp, shape=(V.value + 1,)).copy()}
+    ne = int(out["row_ptr"][-1])
+    out["col"] = np.ctypeslib.as_array(col, shape=(max(1, ne),))[:ne].copy()
+    for p in (coo, rp, col):
+        R.ref_read_free(ctypes.cast(p, ctypes.c_void_p))
+    return out
+
+
+def ref_load_graph(path: str):
+    """bernaschi load_graph on `path` (one rank): (nverts, int64[n, 2] raw
+    (u, v) pairs in file order)."""
+    R = ctypes.CDLL(REF_LOADGRAPH_PATH)
+    R.ref_load_graph.restype = ctypes.c_int
+    LP = ctypes.POINTER(ctypes.c_int64)
+    R.ref_load_graph.argtypes = [ctypes.c_char_p, LP, ctypes.POINTER(LP), LP]
+    R.ref_free.argtypes = [ctypes.c_void_p]
+    n, nv, e = ctypes.c_int64(), ctypes.c_int64(), LP()
+    R.ref_load_graph(path.encode(), ctypes.byref(n), ctypes.byref(e), ctypes.byref(nv))
+    pairs = np.ctypeslib.as_array(e, shape=(max(1, 2 * n.value),))[: 2 * n.value].reshape(-1, 2).copy()
+    R.ref_free(ctypes.cast(e, ctypes.c_void_p))
+    return int(nv.value), pairs

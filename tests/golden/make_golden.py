@@ -14,6 +14,12 @@ What it writes (all small, all committed):
   reference's vendored Graph500 generator (compiled by ``oracle/Makefile``
   into ``oracle/_ref/graph500_gen``), symmetrised, loop-free and deduped,
   stored as the sorted upper triangle (u < v): ``du`` = deltas of u, ``v``.
+* ``ref_readers.json`` -- what the reference's own edge-list readers make of
+  the files of ``reader_cases.py``: BFS-4K's ``readGraphHeader`` +
+  ``readSTD`` + ``Graph::ToCSR`` (compiled into ``oracle/_ref/libref_read.so``)
+  and bernaschi's ``load_graph`` (``oracle/_ref/libref_loadgraph.so``):
+  vertex count, direction, the COO list in the reader's order and the CSR,
+  as SHA-256 digests plus the full arrays of the small files.
 * ``ref_bfs_*.json`` -- outputs of the reference's own CPU BFS
   (``Graph::bfs``, BFS-4K/src/host/graph.cpp:83-97, compiled into
   ``oracle/_ref/libref_bfs.so``) on the ER workload (65,536 vertices,
@@ -85,14 +91,53 @@ def tiny_graphs():
     return g
 
 
+def sha_i32(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<i4").tobytes()).hexdigest()
+
+
+def reader_fixtures():
+    """ref_readers.json from the reference readers run on reader_cases.py."""
+    sys.path.insert(0, HERE)
+    import reader_cases
+    out = []
+    with tempfile.TemporaryDirectory() as td:
+        for name, text, readers in reader_cases.cases():
+            p = os.path.join(td, name)
+            with open(p, "w") as f:
+                f.write(text)
+            rec = {"name": name, "readers": list(readers)}
+            r = oracle.ref_read_graph(p)
+            small = len(r["coo"]) <= 64
+            rec["bfs4k"] = {"V": r["V"], "direction": r["direction"],
+                            "coo_n": int(len(r["coo"])), "coo_sha256": sha_i32(r["coo"]),
+                            "row_ptr_sha256": sha_i32(r["row_ptr"]),
+                            "col_sha256": sha_i32(r["col"])}
+            if small:
+                rec["bfs4k"].update(coo=r["coo"].tolist(), row_ptr=r["row_ptr"].tolist(),
+                                    col=r["col"].tolist())
+            if "bernaschi" in readers:
+                nv, pairs = oracle.ref_load_graph(p)
+                rec["bernaschi"] = {"nverts": nv, "n": int(len(pairs)),
+                                    "pairs_sha256": sha_i32(pairs)}
+                if small:
+                    rec["bernaschi"]["pairs"] = pairs.tolist()
+            out.append(rec)
+    json.dump(out, open(os.path.join(HERE, "ref_readers.json"), "w"), indent=1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("FASTCON_REFERENCE", ""),
                     help="root of the reference tree")
+    ap.add_argument("--only", default=None, choices=["readers"],
+                    help="write only this fixture")
     args = ap.parse_args()
     if not args.ref or not os.path.isdir(args.ref):
         sys.exit("reference tree not found; pass --ref")
     oracle.build(args.ref)
+    if args.only == "readers":
+        reader_fixtures()
+        return
 
     # 1. known-answer rows
     lines = open(os.path.join(args.ref, STATS)).read().splitlines()
@@ -180,6 +225,9 @@ def main():
                      "row_ptr": [int(x) for x in rp], "col": [int(x) for x in col],
                      "sources": [int(x) for x in srcs], "levels": dist.tolist()})
     json.dump(tiny, open(os.path.join(HERE, "ref_bfs_tiny.json"), "w"))
+
+    # 5. the edge-list readers
+    reader_fixtures()
     print("fixtures written to", HERE)
 
 
