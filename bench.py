@@ -231,20 +231,144 @@ def make_workload_cpu(cfg, nthreads, only_graphs=None):
     return csrs, np.concatenate(gi), np.concatenate(ss), np.concatenate(ts)
 
 
-def cpu_queries(csrs, gi, s, t, idx, nthreads):
-    """Run queries idx with the reference's CPU path (full BFS per query)."""
+def cpu_queries(csrs, gi, s, t, idx, nthreads, with_conn=False):
+    """Run queries idx with the reference's CPU path (full BFS per query):
+    hops, or (connected, hops) with with_conn."""
     import oracle
+    conn = np.zeros(len(idx), np.int32)
     hops = np.zeros(len(idx), np.int32)
     if gi is None:
         rp, col = csrs[0]
-        _, h, _ = oracle.stcon_batch(rp, col, s[idx], t[idx], nthreads=nthreads)
-        return h
+        c, h, _ = oracle.stcon_batch(rp, col, s[idx], t[idx], nthreads=nthreads)
+        return (c, h) if with_conn else h
     for g in np.unique(gi[idx]):
         m = gi[idx] == g
         rp, col = csrs[g]
-        _, h, _ = oracle.stcon_batch(rp, col, s[idx][m], t[idx][m], nthreads=nthreads)
+        c, h, _ = oracle.stcon_batch(rp, col, s[idx][m], t[idx][m], nthreads=nthreads)
+        conn[m] = c
         hops[m] = h
-    return hops
+    return (conn, hops) if with_conn else hops
+
+
+def cpu_single_thread(csrs, gi, s, t, min_seconds=6.0, max_queries=8):
+    """The same CPU path on one thread, a few queries of the workload."""
+    done, t0 = 0, time.perf_counter()
+    while True:
+        cpu_queries(csrs, gi, s, t, np.array([done % len(s)]), 1)
+        done += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds or done >= max_queries:
+            break
+    return {"value": done / el, "unit": UNIT, "cores": 1, "sample": f"{done} queries ({el:.1f} s)"}
+
+
+def cpu_model():
+    """CPU model name of the host (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def same_csr(G, csr):
+    """Device CSR of G equal to the oracle's CSR of the same graph."""
+    if csr is None:
+        return True
+    rp, col = G.csr()
+    return bool(len(rp) == len(csr[0]) and (rp == csr[0]).all() and len(col) == len(csr[1])
+                and (col == csr[1]).all())
+
+
+def plain_bfs_block(fc, G, peak, nsrc=4, reps=5):
+    """Plain expansion: full level-synchronous top-down BFS of G (the plain
+    schedule, the library's default BFS engine) from nsrc sources next to
+    the three-quarter point of the degree order; device time per call from
+    the library's CUDA events.  Algorithmic bytes = 8 per adjacency entry
+    read + 20 per reached vertex (the library's statistics), so frac is the
+    effective-byte fraction of the HBM peak."""
+    rp, _ = G.csr_row_ptr()
+    deg = np.diff(rp)
+    order = np.argsort(deg, kind="stable")
+    srcs = [int(order[len(deg) // 2 + len(deg) // 4 + k]) for k in range(nsrc)]
+    o = fc.make_opts(sched=fc.SCHED_PLAIN)
+    for _ in range(2):
+        G.bfs_levels(srcs[0], o)
+    per = []
+    tot_ms, tot_bytes, tot_entries = 0.0, 0, 0
+    lev0 = None
+    for src in srcs:
+        ms = []
+        for _ in range(reps):
+            lev, st = G.bfs_levels(src, o, stats=True)
+            ms.append(st["gpu_ms"])
+        if lev0 is None:
+            lev0 = lev
+        m = statistics.median(ms)
+        tot_ms += m
+        tot_bytes += st["alg_bytes"]
+        tot_entries += st["edges_inspected"]
+        per.append({"source": src, "ms": m, "levels": int(lev.max()) + 1,
+                    "entries": int(st["edges_inspected"]), "reached": int((lev >= 0).sum())})
+    achieved = tot_bytes / 1e9 / (tot_ms / 1e3)
+    return {"form": "full BFS, plain schedule (level-synchronous, top-down), library default engine",
+            "ms": tot_ms / len(srcs), "alg_bytes": tot_bytes / len(srcs),
+            "achieved_gbs": achieved, "peak": peak, "frac": achieved / peak,
+            "gteps_entries": tot_entries / (tot_ms * 1e6), "sources": per,
+            "bytes_rule": "8 per adjacency entry read + 20 per reached vertex",
+            "_source": srcs[0], "_levels": lev0}
+
+
+def ka16_block(fc):
+    """The reference's only published ST-CON run, replayed: Graph500 R-MAT
+    scale 16 (seeds 670021781 / 1422323141) and its 100 (RED-V, BLUE-V)
+    pairs, as the reference ran them (one query per call, DEPTH =
+    ceil(hops / 2), make_stcon's answer) and batched."""
+    gdir = os.path.join(ROOT, "tests", "golden")
+    z = np.load(os.path.join(gdir, "rmat16_graph500_edges.npz"))
+    u = np.cumsum(z["du"].astype(np.int64)).astype(np.int32)
+    v = z["v"].astype(np.int32)
+    ka = json.load(open(os.path.join(gdir, "stcon_known_answer.json")))
+    rows = ka["rows"]
+    red = np.array([r["red"] for r in rows], np.int32)
+    blue = np.array([r["blue"] for r in rows], np.int32)
+    depth_ref = np.array([r["depth"] for r in rows], np.int32)
+    G = fc.Graph.from_edges(u, v, 1 << 16)
+    for k in range(10):
+        G.stcon_depth(int(red[k]), int(blue[k]))
+    t0 = time.perf_counter()
+    depth = np.array([G.stcon_depth(int(a), int(b)) for a, b in zip(red, blue)], np.int32)
+    single_s = time.perf_counter() - t0
+    fc.stcon_batch(G, red, blue)
+    t0 = time.perf_counter()
+    reps = 20
+    for _ in range(reps):
+        conn, hops = fc.stcon_batch(G, red, blue)
+    batch_s = (time.perf_counter() - t0) / reps
+    bdepth = np.where(conn != 0, (hops + 1) // 2, -1)
+    G.free()
+    return {"workload": "Graph500 R-MAT scale 16, edgefactor 16, 100 (RED-V, BLUE-V) pairs of "
+                        "the reference's logged run",
+            "single_query": {"ms_per_query": 1000 * single_s / len(red),
+                             "conps": len(red) / single_s,
+                             "form": "fc_stcon_depth per query from Python, host to host"},
+            "batched": {"queries_per_s": len(red) / batch_s,
+                        "form": "fc_stcon_batch of the 100 pairs, host arrays"},
+            "depth_match": f"{int((depth == depth_ref).sum())}/{len(red)}",
+            "batched_depth_match": f"{int((bdepth == depth_ref).sum())}/{len(red)}",
+            "published": {"ms_per_query": 0.57856, "conps": 1756.99, "hardware": "RTX 2070",
+                          "source": "bernaschi/ST_CONN_ONE_ATOMIC/current-st/st-conn/data/"
+                                    "st_stats_20200418_140644:112-116"}}
 
 
 def cpu_rate(csrs, gi, s, t, nthreads, min_seconds=10.0, max_queries=None, order=None):
@@ -481,36 +605,66 @@ def run_fastcon(args, cfg):
     single = {"value": plain_n / single_s, "unit": UNIT, "sample": plain_n,
               "form": "fc_stcon per query (one persistent launch each)"}
 
+    # plain expansion: one full top-down BFS of the workload's graph
+    plain_bfs = plain_bfs_block(fc, Gs[0], peak) if gi is None else None
+    # the reference's only published run, replayed (Graph500 R-MAT 16)
+    ka16 = ka16_block(fc)
+
     if rank == 0:
         cpu = None
+        oracle_check = None
         if ws == 1:
             nthreads = os.cpu_count() or 1
-            # the oracle checks a sample of this very workload, then is timed
-            cs = np.arange(0, nq, max(1, nq // 16))
-            graphs_needed = None if gi is None else set(int(x) for x in np.unique(gi[cs]))
-            if gi is None:
-                csrs = [Gs[0].csr()]
-            else:
-                csrs = [Gs[k].csr() if k in graphs_needed else None for k in range(len(Gs))]
-            want = cpu_queries(csrs, gi, s, t, cs, nthreads)
-            exact = exact and bool((hops_gpu[cs] == want).all())
-            rate, done, el = cpu_rate(csrs, gi, s, t, nthreads, min_seconds=10.0,
-                                      max_queries=4 * nthreads, order=cs)
-            cpu = {"value": rate, "unit": UNIT, "cores": nthreads, "kind": "port",
-                   "sample": f"{done} queries of the workload ({el:.1f} s), one full BFS from s "
-                             "per query (Graph::bfs restated in oracle/fc_oracle.c)"}
+            # every answer of this very workload against the oracle (outside
+            # the timed region), on a CSR the oracle builds itself from the
+            # same generator -- so the device ingest is checked too
+            t0 = time.perf_counter()
+            csrs, gi_c, s_c, t_c = make_workload_cpu(cfg, nthreads)
+            build_s = time.perf_counter() - t0
+            csr_match = all(same_csr(G, c) for G, c in zip(Gs, csrs))
+            csr_match = csr_match and bool((s_c == s).all() and (t_c == t).all())
+            conn_gpu = d_c.cpu().numpy()
+            t0 = time.perf_counter()
+            want_c, want_h = cpu_queries(csrs, gi, s, t, np.arange(nq), nthreads, with_conn=True)
+            el = time.perf_counter() - t0
+            mism = int(((hops_gpu != want_h) | (conn_gpu != want_c)).sum())
+            exact = exact and mism == 0
+            oracle_check = {"checked": f"{nq}/{nq}", "mismatches": mism, "csr_match": csr_match,
+                            "oracle": "Graph::bfs restated in oracle/fc_oracle.c, one full BFS "
+                                      "from s per query, on the oracle's own CSR",
+                            "oracle_csr_build_s": round(build_s, 1)}
+            if plain_bfs is not None:
+                src = plain_bfs.pop("_source")
+                lev_gpu = plain_bfs.pop("_levels")
+                import oracle
+                lev_cpu, _ = oracle.bfs_levels(csrs[0][0], csrs[0][1], src)
+                plain_bfs["levels_exact"] = bool((lev_gpu == lev_cpu).all())
+                exact = exact and plain_bfs["levels_exact"]
+            one = cpu_single_thread(csrs, gi, s, t)
+            cpu = {"value": nq / el, "unit": UNIT, "cores": nthreads, "kind": "port",
+                   "sample": f"all {nq} queries of the workload ({el:.1f} s), one full BFS from s "
+                             "per query (Graph::bfs restated in oracle/fc_oracle.c)",
+                   "cpu_model": cpu_model(), "single_thread": one}
+        elif plain_bfs is not None:
+            plain_bfs.pop("_source")
+            plain_bfs.pop("_levels")
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "config": dict(config_desc(args.config, cfg, nq), engine="batched",
                            sched=args.sched, parallelism=f"replicas{ws}"),
-            "exact": exact,
+            "exact": exact, "oracle_check": oracle_check,
             "gteps_inspected": ins / args.steps / (ms / args.steps / 1000.0) / 1e9,
-            # the reference's TEPS numerator (count_visited_edges): edges of the
-            # visited vertices counted once, i.e. half their degree sum
-            "gteps_graph500": vadj / 2 / args.steps / (ms / args.steps / 1000.0) / 1e9,
             "edges_inspected_per_step": ins / args.steps,
+            # the reference's TEPS numerator (count_visited_edges, S/adj_func.c:334-357)
+            # counts every edge of every visited vertex, almost none of which an
+            # early-exit search reads: context only, not a speed
+            "visited_edges_convention": {
+                "gteps": vadj / 2 / args.steps / (ms / args.steps / 1000.0) / 1e9,
+                "note": "edges of the visited vertices per second (Graph500 count_visited_edges); "
+                        "most were never read"},
+            "plain_bfs": plain_bfs, "ka16": ka16,
             "plain": plain, "one_launch_per_query": single, "schedules": schedules,
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": launches * args.steps,

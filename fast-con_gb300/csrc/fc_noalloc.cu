@@ -13,17 +13,28 @@
 //
 // The working memory of the queries (a status byte and a visit-log entry per
 // vertex for each of NOALLOC_SLOTS CTAs) is one file-scope __device__ array of
-// NOALLOC_BYTES (20 MiB).  It exists in every GPU's memory from the moment the
-// library is loaded there until the process exits.  Limits and rules:
+// NOALLOC_BYTES (20 MiB).  Once the library's device code is loaded on a GPU,
+// the array occupies that GPU's memory until the process exits.  Limits and
+// rules:
 //   * graphs of at most NOALLOC_MAX_NV (1,048,576) vertices; larger ones are
 //     rejected with FC_ERR_INVALID;
 //   * the array is shared by every call and keeps the previous call's
 //     contents, so each call first re-initialises the part it uses; two calls
 //     whose kernels overlap on the GPU (different streams, or threads racing)
 //     race on the array and must be serialised by the caller;
-//   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (once per device, with that device current); make
-//     that first call before any stream capture begins.
+//   * set-up happens in the first call on a device (and again if that
+//     device's CUDA context was destroyed and re-created, e.g. after
+//     cudaDeviceReset): with that device current it makes sure the library's
+//     device code is loaded and looks up the array's device address with
+//     cudaGetSymbolAddress.  Under lazy module loading (CUDA_MODULE_LOADING=
+//     LAZY, the CUDA 12+ default) loading the code is what places the array
+//     in device memory, so that first call may allocate: make it before the
+//     caller reserves its device memory and before any stream capture begins
+//     (or run with CUDA_MODULE_LOADING=EAGER).  Later calls allocate nothing;
+//   * sched FC_SCHED_LEARNED runs as FC_SCHED_HEURISTIC here (the network's
+//     weights live in memory the regular entry points allocate).
+#include <cuda.h>  // driver types only: the entry points are fetched through the runtime
+
 #include <mutex>
 
 #include "fastcon.h"
@@ -83,7 +94,7 @@ __global__ void __launch_bounds__(T) k_stcon_noalloc(GraphPair gp, const int32_t
             const int32_t *front = ql_frontier(ql, log, nv, x, &F);
             run_step<T>(MODE_STCON, gp, x, DIR_TD, ql.radius[x], ql.radius[1 - x], front, F, 0, 1,
                         status, nullptr, log, nv, &tc.tail[x], &tc.deg[x], &tc.found,
-                        &tc.inspected, sm);
+                        &tc.inspected, sm, ql.variant);
             __syncthreads();
             if (threadIdx.x == 0) ql_update(ql, tc.found, tc.tail[x], tc.deg[x], tc.inspected);
             __syncthreads();
@@ -102,23 +113,70 @@ __global__ void __launch_bounds__(T) k_stcon_noalloc(GraphPair gp, const int32_t
 }
 
 std::mutex g_setup_mu;
-unsigned char *g_scratch_ptr[64];
+struct DeviceSetup {
+    unsigned long long ctx_id;  // CUDA context the address belongs to (0: unknown)
+    unsigned char *scratch;     // device address of g_noalloc_scratch
+};
+DeviceSetup g_setup[64];
 
-// Device address of the scratch array for the current device (looked up
-// once per device; the host-side symbol itself is not a device address).
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext *);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long *);
+
+// Identifier of the current CUDA context (unique for the process's lifetime),
+// or 0 when the driver cannot tell.  Driver entry points come through the
+// runtime, so the library needs no link against the driver library.
+unsigned long long current_context_id()
+{
+    static PfnCtxGetCurrent get_current = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) {
+        resolved = true;
+        cudaDriverEntryPointQueryResult q;
+        void *f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<PfnCtxGetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PfnCtxGetId>(f);
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx ||
+        get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
+// Device address of the scratch array for the current device (the host-side
+// symbol itself is not a device address).  Set-up runs on the first call on
+// a device and again whenever that device's context has changed: it loads
+// the module (cudaFuncGetAttributes), which also makes the context current,
+// then looks the symbol up.
 int scratch_for_device(int dev, unsigned char **out)
 {
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
+    DeviceSetup &d = g_setup[dev];
+    unsigned long long id = current_context_id();
+    if (!d.scratch || id == 0 || id != d.ctx_id) {
+        cudaFuncAttributes fa;
+        cudaError_t e = cudaFuncGetAttributes(&fa, k_stcon_noalloc<FC_BLOCK>);
+        if (e != cudaSuccess) {
+            fc_set_last_cuda_error(e, "cudaFuncGetAttributes(k_stcon_noalloc)", __FILE__, __LINE__);
+            return FC_ERR_CUDA;
+        }
         void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
             fc_set_last_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
             return FC_ERR_CUDA;
         }
-        g_scratch_ptr[dev] = static_cast<unsigned char *>(p);
+        d.scratch = static_cast<unsigned char *>(p);
+        d.ctx_id = current_context_id();
     }
-    *out = g_scratch_ptr[dev];
+    *out = d.scratch;
     return FC_OK;
 }
 
@@ -140,6 +198,10 @@ extern "C" int fc_stcon_batch_noalloc(const int32_t *d_row_ptr, const int32_t *d
         set_error("fc_stcon_batch_noalloc: %d vertices; this entry point handles 1 to %d "
                   "(its working memory is a fixed %zu-byte device array)",
                   nv, NOALLOC_MAX_NV, NOALLOC_BYTES);
+        return FC_ERR_INVALID;
+    }
+    if (sched != FC_SCHED_PLAIN && sched != FC_SCHED_HEURISTIC && sched != FC_SCHED_LEARNED) {
+        set_error("fc_stcon_batch_noalloc: sched %d is not an FC_SCHED_* value", sched);
         return FC_ERR_INVALID;
     }
     if (nq == 0) return FC_OK;
@@ -169,8 +231,10 @@ extern "C" int fc_stcon_batch_noalloc(const int32_t *d_row_ptr, const int32_t *d
         gp.rev.row_ptr = d_rrow_ptr;
         gp.rev.col = d_rcol;
     }
+    // the learned schedule needs weights from allocated memory: heuristic here
+    const int run_sched = sched == FC_SCHED_LEARNED ? FC_SCHED_HEURISTIC : sched;
     k_stcon_noalloc<FC_BLOCK><<<NOALLOC_SLOTS, FC_BLOCK, 0, (cudaStream_t)stream>>>(
-        gp, d_s, d_t, nq, d_connected, d_hops, sched, scratch);
+        gp, d_s, d_t, nq, d_connected, d_hops, run_sched, scratch);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         fc_set_last_cuda_error(e, "k_stcon_noalloc launch", __FILE__, __LINE__);

@@ -261,14 +261,22 @@ int fc_stcon_batch_scripted(fc_graph *g, const int32_t *d_s, const int32_t *d_t,
  * and forbids allocator calls afterwards, or a plug-in inside a framework
  * that owns the device memory.  The caller passes the graph as device CSR
  * arrays (d_rrow_ptr / d_rcol: reverse CSR of a directed graph, or NULL for
- * a symmetric one) and device arrays for queries and results; sched is an
- * FC_SCHED_* value.  Working memory is a fixed 20 MiB device array inside the
- * library (held on every GPU that loads it until exit), so graphs are limited
- * to 1,048,576 vertices (larger: FC_ERR_INVALID).  Calls share that array:
- * calls whose kernels overlap on the GPU race and must be serialised.  The
- * first call on a device looks up the array's address (once per device); make
- * it before any stream capture.  Asynchronous on `stream` (a cudaStream_t);
- * out-of-range query ids give connected = 0, hops = -2. */
+ * a symmetric one) and device arrays for queries and results.  sched is
+ * FC_SCHED_PLAIN or FC_SCHED_HEURISTIC; FC_SCHED_LEARNED is accepted and runs
+ * as FC_SCHED_HEURISTIC (the network's weights live in allocated memory);
+ * other values give FC_ERR_INVALID.  Working memory is a fixed 20 MiB device
+ * array inside the library (held on every GPU that loads the library's
+ * device code, until exit), so graphs are limited to 1,048,576 vertices
+ * (larger: FC_ERR_INVALID).  Calls share that array: calls whose kernels
+ * overlap on the GPU race and must be serialised.  The first call on a
+ * device (and the first after that device's context was re-created) sets up:
+ * it loads the library's device code if the CUDA runtime loads it lazily
+ * (CUDA_MODULE_LOADING=LAZY, the default), which is when the array is placed
+ * in device memory, and looks up the array's address.  That first call may
+ * therefore allocate: make it before reserving device memory and before any
+ * stream capture, or set CUDA_MODULE_LOADING=EAGER.  Asynchronous on
+ * `stream` (a cudaStream_t); out-of-range query ids give connected = 0,
+ * hops = -2. */
 int fc_stcon_batch_noalloc(const int32_t *d_row_ptr, const int32_t *d_col, int32_t nv, int64_t ne,
                            const int32_t *d_rrow_ptr, const int32_t *d_rcol, const int32_t *d_s,
                            const int32_t *d_t, int32_t nq, int32_t *d_connected, int32_t *d_hops,
