@@ -689,8 +689,10 @@ def run_bfs(args, cfg):
     deg = np.diff(rp)
     src = int(np.argsort(deg)[len(deg) // 2 + len(deg) // 4])
     o = fc.make_opts(sched=fc.SCHED_PLAIN if args.bfs == "plain" else fc.SCHED_HEURISTIC,
-                     engine=fc.ENGINE_HOSTLOOP if args.engine == "hostloop"
-                     else fc.ENGINE_PERSISTENT)
+                     engine={"hostloop": fc.ENGINE_HOSTLOOP, "persistent": fc.ENGINE_PERSISTENT,
+                             "auto": fc.ENGINE_AUTO}[args.engine],
+                     vertex_order={"auto": fc.ORDER_AUTO, "given": fc.ORDER_GIVEN,
+                                   "degree": fc.ORDER_DEGREE}[args.order])
     ms = []
     for k in range(args.warmup + args.steps):
         lev, st = G.bfs_levels(src, o, stats=True)
@@ -698,7 +700,8 @@ def run_bfs(args, cfg):
             ms.append(st["gpu_ms"])
     reached = lev >= 0
     entries = int(deg[reached].sum())
-    print(json.dumps({"bfs": args.bfs, "engine": args.engine, "workload": args.config,
+    print(json.dumps({"bfs": args.bfs, "engine": args.engine, "order": args.order,
+                      "workload": args.config,
                       "source": src, "levels": np.bincount(lev[reached]).tolist(),
                       "ms": min(ms), "entries_inspected": int(st["edges_inspected"]),
                       "gteps_entries": entries / (min(ms) * 1e6)}))
@@ -714,8 +717,10 @@ def main():
     ap.add_argument("--sched", default="learned", choices=["heuristic", "plain", "learned"])
     ap.add_argument("--bfs", default=None, choices=["plain", "heuristic"],
                     help="time one full BFS of the workload's graph instead of the batch")
-    ap.add_argument("--engine", default="hostloop", choices=["hostloop", "persistent"],
-                    help="engine of --bfs")
+    ap.add_argument("--engine", default="auto", choices=["auto", "hostloop", "persistent"],
+                    help="engine of --bfs (auto: the plain BFS engine for --bfs plain)")
+    ap.add_argument("--order", default="auto", choices=["auto", "given", "degree"],
+                    help="vertex numbering of the plain BFS engine (--bfs plain --engine auto)")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     import oracle

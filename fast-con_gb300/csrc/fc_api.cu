@@ -23,6 +23,10 @@ struct fc_graph {
     int directed;
     int32_t *row_ptr, *col;    // forward CSR
     int32_t *rrow_ptr, *rcol;  // reverse CSR (same pointers when undirected)
+    // degree-ordered copy for the plain BFS engine: built on first use;
+    // layout_state 0 = not decided, 1 = built, 2 = the graph keeps its numbering
+    fc::BfsLayout *bfs_layout;
+    int layout_state;
 };
 
 namespace {
@@ -409,6 +413,7 @@ int fc_graph_get_csr(const fc_graph *g, int32_t *row_ptr, int32_t *col)
 void fc_graph_free(fc_graph *g)
 {
     if (!g) return;
+    fc::bfs_layout_free(g->bfs_layout);
     if (g->rrow_ptr && g->rrow_ptr != g->row_ptr) cudaFree(g->rrow_ptr);
     if (g->rcol && g->rcol != g->col) cudaFree(g->rcol);
     cudaFree(g->row_ptr);
@@ -426,6 +431,23 @@ int fc_bfs_levels_ex(fc_graph *g, int32_t s, int32_t *levels, const fc_opts *opt
     fc_opts o = opts ? *opts : default_opts();
     CtxLock L;
     if (!L.c) return L.rc;
+    if (o.engine == FC_ENGINE_AUTO && o.sched == FC_SCHED_PLAIN) {
+        // the visited-bitmap engine; degree-ordered numbering unless the
+        // caller asks for the graph's own, or (auto) the graph has no hubs
+        const fc::BfsLayout *lay = nullptr;
+        if (o.vertex_order != FC_ORDER_GIVEN) {
+            if (g->layout_state == 0 || (g->layout_state == 2 && o.vertex_order == FC_ORDER_DEGREE)) {
+                fc::BfsLayout *nl = nullptr;
+                int rc = fc::bfs_layout_build(pair_of(g), &nl, pick_stream(opts, L.c),
+                                              o.vertex_order == FC_ORDER_AUTO);
+                if (rc) return rc;
+                g->bfs_layout = nl;
+                g->layout_state = nl ? 1 : 2;
+            }
+            lay = g->bfs_layout;
+        }
+        return fc::engine_bfs_plain(L.c, pair_of(g), lay, s, levels, stats, pick_stream(opts, L.c));
+    }
     return fc::engine_bfs(L.c, pair_of(g), s, levels, o, stats, pick_stream(opts, L.c));
 }
 

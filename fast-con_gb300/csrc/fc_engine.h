@@ -89,6 +89,17 @@ struct DevCtx {
     // staging of host-array batches (queries in, answers out)
     int32_t *b_stage = nullptr;
     size_t b_stage_cap = 0;
+    // plain BFS engine (fc_bfs.cu): visited bitmap, levels and queue in the
+    // search's numbering, levels in the caller's numbering, counters, row jobs
+    unsigned *bfs_bm = nullptr;
+    int32_t *bfs_lev = nullptr;
+    int32_t *bfs_q = nullptr;
+    int32_t *bfs_out = nullptr;
+    size_t bfs_nv = 0;
+    void *bfs_ctr = nullptr;
+    void *h_bfs_ctr = nullptr;
+    int2 *bfs_jobs = nullptr;
+    int bfs_jcap = 0;
 };
 
 // Device staging for a host-array batch of n queries: 5n ints, kept between
@@ -99,6 +110,14 @@ DevCtx *get_ctx(int *err);
 
 int engine_bfs(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_levels,
                const fc_opts &o, fc_stats *st, cudaStream_t stream);
+
+// Plain (top-down, level-synchronous) BFS on the visited-bitmap engine of
+// fc_bfs.cu; L (nullable) is the graph's degree-ordered copy.
+struct BfsLayout;
+int bfs_layout_build(const GraphPairH &gp, BfsLayout **out, cudaStream_t st, int only_if_skewed);
+void bfs_layout_free(BfsLayout *L);
+int engine_bfs_plain(DevCtx *c, const GraphPairH &gp, const BfsLayout *L, int32_t s,
+                     int32_t *h_levels, fc_stats *st, cudaStream_t stream);
 
 int engine_stcon(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int32_t *conn,
                  int32_t *hops, const fc_opts &o, fc_stats *st, cudaStream_t stream);

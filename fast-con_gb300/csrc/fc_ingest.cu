@@ -151,6 +151,11 @@ static int exclusive_scan(const In *in, long long n, long long *out, cudaStream_
     return FC_OK;
 }
 
+int scan_i32(const int32_t *in, long long n, long long *out, cudaStream_t st)
+{
+    return exclusive_scan<int32_t>(in, n, out, st);
+}
+
 // ---------------------------------------------------------------------------
 // count / scatter
 // ---------------------------------------------------------------------------

@@ -30,6 +30,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_IO, ERR_FORMAT, ERR_TIMEOUT, ERR_OVERFLO
 INGEST_DIRECTED, INGEST_KEEP_LOOPS, INGEST_KEEP_DUPS = 1, 2, 4
 SCHED_PLAIN, SCHED_HEURISTIC, SCHED_LEARNED = 0, 1, 2
 ENGINE_AUTO, ENGINE_HOSTLOOP, ENGINE_PERSISTENT, ENGINE_BATCHED = 0, 1, 2, 3
+ORDER_AUTO, ORDER_GIVEN, ORDER_DEGREE = 0, 1, 2
 
 # Every symbol include/fastcon.h declares.
 EXPORTS = [
@@ -57,7 +58,8 @@ class Opts(ctypes.Structure):
                 ("max_slots", ctypes.c_int32), ("stream", ctypes.c_void_p),
                 ("cta_work_k", ctypes.c_int32), ("variant", ctypes.c_int32),
                 ("tile_entries", ctypes.c_int32), ("job_entries", ctypes.c_int32),
-                ("private_variant", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("private_variant", ctypes.c_int32), ("vertex_order", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
 
 class Stats(ctypes.Structure):
@@ -157,9 +159,11 @@ def _i32(a):
 
 def make_opts(sched=SCHED_HEURISTIC, engine=ENGINE_AUTO, block=0, ctas_per_sm=0, use_graph=0,
               max_slots=0, stream=None, cta_work_k=0, variant=0, tile_entries=0,
-              job_entries=0, private_variant=0) -> Opts:
+              job_entries=0, private_variant=0, vertex_order=0) -> Opts:
     """variant: 0 = chosen by the schedule, 1 hybrid, 2 warp-centric, 3 lane per row;
-    tile_entries / job_entries: work-sharing tile and row-job sizes (0 = defaults)."""
+    tile_entries / job_entries: work-sharing tile and row-job sizes (0 = defaults);
+    vertex_order: numbering of the plain BFS engine (ORDER_AUTO / ORDER_GIVEN /
+    ORDER_DEGREE)."""
     o = Opts()
     lib().fc_opts_init(ctypes.byref(o))
     o.sched, o.engine, o.block, o.ctas_per_sm = sched, engine, block, ctas_per_sm
@@ -169,6 +173,7 @@ def make_opts(sched=SCHED_HEURISTIC, engine=ENGINE_AUTO, block=0, ctas_per_sm=0,
     o.variant = variant
     o.tile_entries, o.job_entries = tile_entries, job_entries
     o.private_variant = private_variant
+    o.vertex_order = vertex_order
     return o
 
 

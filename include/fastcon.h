@@ -82,8 +82,16 @@ typedef struct fc_opts {
     int32_t private_variant; /* work-sharing engine: expansion variant of the
                              steps an owner CTA runs alone (same codes as
                              `variant`; 0 = the schedule's choice)          */
-    int32_t reserved[3];
+    int32_t vertex_order; /* plain BFS engine (FC_ENGINE_AUTO with
+                             FC_SCHED_PLAIN in fc_bfs_levels_ex): FC_ORDER_* */
+    int32_t reserved[2];
 } fc_opts;
+
+/* ---- vertex numbering of the plain BFS engine ---------------------------- */
+#define FC_ORDER_AUTO   0  /* degree-ordered copy when the graph has hubs
+                              (a vertex of degree >= 256), else as given      */
+#define FC_ORDER_GIVEN  1  /* search the caller's numbering                   */
+#define FC_ORDER_DEGREE 2  /* always search a degree-ordered copy             */
 
 typedef struct fc_stats {
     int64_t edges_inspected;  /* adjacency entries read by expansion steps   */
@@ -179,7 +187,11 @@ void fc_graph_free(fc_graph *g);
 /* Full BFS level array from s (host output, nv entries, -1 = unreachable).
  * Replaces cudaGraph::Reset + cudaBFS4K (K/src/device/BFS_WorkEfficient.cu:
  * 81-133) whose result is left in devDistance, and Graph::BfsInit + bfs on
- * the host (K/src/host/graph.cpp:70-97). */
+ * the host (K/src/host/graph.cpp:70-97).  With FC_ENGINE_AUTO and
+ * FC_SCHED_PLAIN the search runs on the plain BFS engine: top-down levels
+ * in one cooperative launch, visited bits in a bitmap, and (opts.vertex_order)
+ * on a degree-ordered copy of the graph that the first such call builds and
+ * the graph handle keeps (as much device memory again as the CSR). */
 int fc_bfs_levels(fc_graph *g, int32_t s, int32_t *levels);
 int fc_bfs_levels_ex(fc_graph *g, int32_t s, int32_t *levels, const fc_opts *opts,
                      fc_stats *stats);

@@ -52,6 +52,11 @@ def test_tiny_graphs_bfs_levels(fastcon_lib, tiny_golden):
                 for i, s in enumerate(g["sources"]):
                     assert G.bfs_levels(s, o).tolist() == g["levels"][i], (g["name"], eng, sch, s)
                     assert G2.bfs_levels(s, o).tolist() == g["levels"][i]
+        # the plain BFS engine, in the graph's numbering and degree-ordered
+        for order in (fc.ORDER_GIVEN, fc.ORDER_DEGREE):
+            o = fc.make_opts(sched=fc.SCHED_PLAIN, vertex_order=order)
+            for i, s in enumerate(g["sources"]):
+                assert G.bfs_levels(s, o).tolist() == g["levels"][i], (g["name"], order, s)
 
 
 def test_tiny_graphs_stcon_all_pairs(fastcon_lib, tiny_golden):
@@ -99,9 +104,13 @@ def test_er_device_ingest_is_canonical(er_graph, er_golden):
 
 @pytest.mark.parametrize("engine,sched", [("hostloop", "plain"), ("persistent", "plain"),
                                           ("persistent", "heuristic"), ("hostloop", "heuristic"),
-                                          ("batched", "plain"), ("batched", "heuristic")])
+                                          ("batched", "plain"), ("batched", "heuristic"),
+                                          ("auto", "plain")])
 def test_er_bfs_levels_match_reference(fastcon_lib, er_graph, er_golden, engine, sched):
     o = opts(fastcon_lib, engine, sched)
+    if engine == "auto":  # the plain BFS engine, degree-ordered copy
+        o = fastcon_lib.make_opts(sched=fastcon_lib.SCHED_PLAIN,
+                                  vertex_order=fastcon_lib.ORDER_DEGREE)
     bu = 0
     for i, s in enumerate(er_golden["s"]):
         lev, st = er_graph.bfs_levels(s, o, stats=True)
@@ -515,3 +524,46 @@ def test_entries_read_accounting(fastcon_lib, oracle_mod):
             got, st = G.bfs_levels(src, o, stats=True)
             assert (got == lev).all()
             assert st["edges_inspected"] == want, (eng, src, st["edges_inspected"], want)
+
+
+# --------------------------------------------------------------------------
+# the plain BFS engine (visited bitmap, degree-ordered copy): levels against
+# the oracle on hub graphs, directed graphs, deep paths, grids, isolated
+# vertices; statistics follow the algorithmic-byte rule
+# --------------------------------------------------------------------------
+def test_plain_bfs_engine(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    cases = []
+    u, v = graphs.rmat_edges(16, 8 << 16, seed=81, perm_seed=82)
+    cases.append(("rmat16", 1 << 16, u, v, 0))
+    cases.append(("rmat15_directed", 1 << 15, *graphs.rmat_edges(15, 8 << 15, seed=83, perm_seed=84),
+                  fc.INGEST_DIRECTED))
+    nv = 90001  # a 60,000-leaf hub (row jobs), a path, random edges; nv not a multiple of 32
+    rng = np.random.default_rng(85)
+    u = np.concatenate([np.zeros(60000), np.arange(60001, 90000),
+                        rng.integers(0, nv, 5000)]).astype(np.int32)
+    v = np.concatenate([np.arange(1, 60001), np.arange(60002, 90001),
+                        rng.integers(0, nv, 5000)]).astype(np.int32)
+    cases.append(("hub_path", nv, u, v, 0))
+    cases.append(("path700", 700, np.arange(699), np.arange(1, 700), 0))
+    u, v = graphs.grid_edges(300, 200, 0.05, 5, 7, 6)
+    cases.append(("grid300x200", 60000, u, v, 0))
+    u = rng.integers(0, 50000, 40000).astype(np.int32)  # many isolated vertices
+    v = rng.integers(0, 50000, 40000).astype(np.int32)
+    cases.append(("sparse", 50003, u, v, 0))
+    for name, nv, u, v, flags in cases:
+        G = fc.Graph.from_edges(u, v, nv, flags=flags)
+        rp, col = G.csr()
+        deg = np.diff(rp)
+        srcs = [int(np.argmax(deg)), 0, nv - 1, int(np.argsort(deg)[3 * nv // 4])]
+        for order in (fc.ORDER_AUTO, fc.ORDER_GIVEN, fc.ORDER_DEGREE):
+            o = fc.make_opts(sched=fc.SCHED_PLAIN, vertex_order=order)
+            for src in srcs:
+                want, _ = oracle_mod.bfs_levels(rp, col, src)
+                lev, st = G.bfs_levels(src, o, stats=True)
+                assert (lev == want).all(), (name, order, src)
+                reached = int((want >= 0).sum())
+                assert st["visited"] == reached and st["steps"] == int(want.max()) + 1
+                assert st["edges_inspected"] == int(deg[want >= 0].sum()), (name, order, src)
+                assert st["alg_bytes"] == 20 * reached - 8 + 8 * st["edges_inspected"]
+        G.free()
