@@ -700,7 +700,12 @@ def run_bfs(args, cfg):
             ms.append(st["gpu_ms"])
     reached = lev >= 0
     entries = int(deg[reached].sum())
-    print(json.dumps({"bfs": args.bfs, "engine": args.engine, "order": args.order,
+    trace = None
+    if args.bfs == "plain" and args.engine == "auto":
+        tr = fc.bfs_trace()
+        trace = {"level_us": (tr["level_ns"] / 1e3).round(1).tolist(),
+                 "frontier": tr["frontier"].tolist(), "entries": tr["entries"].tolist()}
+    print(json.dumps({"bfs": args.bfs, "engine": args.engine, "order": args.order, "trace": trace,
                       "workload": args.config,
                       "source": src, "levels": np.bincount(lev[reached]).tolist(),
                       "ms": min(ms), "entries_inspected": int(st["edges_inspected"]),

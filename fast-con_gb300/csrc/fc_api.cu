@@ -451,6 +451,15 @@ int fc_bfs_levels_ex(fc_graph *g, int32_t s, int32_t *levels, const fc_opts *opt
     return fc::engine_bfs(L.c, pair_of(g), s, levels, o, stats, pick_stream(opts, L.c));
 }
 
+int fc_bfs_trace(int32_t *nlevels, int64_t *level_ns, int64_t *frontier, int64_t *entries,
+                 int32_t cap)
+{
+    if (validate_ptr(nlevels, "nlevels")) return FC_ERR_INVALID;
+    CtxLock L;
+    if (!L.c) return L.rc;
+    return fc::engine_bfs_trace(L.c, nlevels, level_ns, frontier, entries, cap);
+}
+
 int fc_bfs_levels(fc_graph *g, int32_t s, int32_t *levels)
 {
     if (validate_ptr(levels, "levels")) return FC_ERR_INVALID;

@@ -255,6 +255,26 @@ int bfs_layout_build(const GraphPairH &gp, BfsLayout **out, cudaStream_t st, int
 // ---------------------------------------------------------------------------
 // the search
 // ---------------------------------------------------------------------------
+struct BfsSnap {  // counters as they stood at a level's last barrier
+    int tail;
+    int nok[2];
+    int pad;
+    unsigned long long deg;
+    unsigned long long reads;
+};
+
+// Per-level record of the last search (the first BFS_TRACE_LEVELS levels):
+// start time from %globaltimer, frontier end in the queue, entries read before
+// the level.  The reference times its levels under DBG_TIME (START_TIMER /
+// STOP_TIMER, S/include/header.h).
+constexpr int BFS_TRACE_LEVELS = 256;
+struct BfsTrace {
+    unsigned long long t0;
+    unsigned long long ns[BFS_TRACE_LEVELS + 1];
+    long long tail[BFS_TRACE_LEVELS + 1];
+    unsigned long long reads[BFS_TRACE_LEVELS + 1];
+};
+
 struct BfsCounters {
     int tail;   // vertices queued (= reached)
     int err;
@@ -263,8 +283,26 @@ struct BfsCounters {
     int nok[2];
     unsigned long long deg;    // degree sum of the queued vertices
     unsigned long long reads;  // adjacency entries read
+    unsigned long long root_deg;
     int levels;                // levels expanded
     int pad;
+    BfsSnap snap[2];           // by barrier generation parity
+    BfsTrace trace;
+};
+
+// Every CTA reads the level's counters from the barrier's snapshot: the
+// fastest CTAs are already claiming the next level's vertices.
+struct SnapBfs {
+    BfsCounters *c;
+    __device__ __forceinline__ void operator()(int p) const
+    {
+        BfsSnap &s = c->snap[p];
+        s.tail = ld_cg(&c->tail);
+        s.nok[0] = ld_cg(&c->nok[0]);
+        s.nok[1] = ld_cg(&c->nok[1]);
+        s.deg = ld_cg_u64(&c->deg);
+        s.reads = ld_cg_u64(&c->reads);
+    }
 };
 
 // Claim through the visited bitmap; the winner writes the level.
@@ -315,6 +353,7 @@ __global__ void k_bfs_root(BfsArgs a, int s)
     c->njobs[0] = c->njobs[1] = 0;
     c->nok[0] = c->nok[1] = 0;
     c->deg = (unsigned long long)(a.row_ptr[s + 1] - a.row_ptr[s]);
+    c->root_deg = c->deg;
     c->reads = 0;
     c->levels = 0;
     c->bar[0] = 0;  // arrivals (a launch that gave up at a barrier may have left some)
@@ -327,7 +366,14 @@ __global__ void __launch_bounds__(T, BFS_MIN_CTAS) k_bfs_plain(BfsArgs a)
     __shared__ int s_nj;
     BfsCounters *c = a.ctr;
     int head = 0, tail = 1, level = 0;
-    unsigned long long dprev = 0, dcur = ld_cg_u64(&c->deg);
+    unsigned long long dprev = 0, dcur = ld_cg_u64(&c->root_deg);
+    const bool tracer = blockIdx.x == 0 && threadIdx.x == 0;
+    if (tracer) {
+        c->trace.t0 = global_timer_ns();
+        c->trace.ns[0] = 0;
+        c->trace.tail[0] = 1;
+        c->trace.reads[0] = 0;
+    }
     while (tail > head) {
         const int F = tail - head;
         const int par = level & 1;
@@ -342,20 +388,27 @@ __global__ void __launch_bounds__(T, BFS_MIN_CTAS) k_bfs_plain(BfsArgs a)
         topdown_step<T>(a.row_ptr, a.col, a.queue + head, F, blockIdx.x, gridDim.x, vis, app, sm,
                         nullptr, TeamSink{a.jobs, a.jcap, &c->njobs[par], &c->nok[par]},
                         team_tile_v<T>(F, (long long)(dcur - dprev)));
-        if (!grid_barrier(c->bar, &c->err, gridDim.x)) return;
-        if (threadIdx.x == 0) s_nj = min(ld_cg(&c->nok[par]), a.jcap);
+        int g = grid_barrier_snap(c->bar, &c->err, gridDim.x, SnapBfs{c});
+        if (g < 0) return;
+        if (threadIdx.x == 0) s_nj = min(ld_cg(&c->snap[g & 1].nok[par]), a.jcap);
         __syncthreads();
         if (s_nj > 0) {  // the same value in every CTA: a uniform barrier
             team_jobs<T>(a.col, a.jobs, s_nj, blockIdx.x, gridDim.x, vis, app, sm, nullptr);
-            if (!grid_barrier(c->bar, &c->err, gridDim.x)) return;
+            g = grid_barrier_snap(c->bar, &c->err, gridDim.x, SnapBfs{c});
+            if (g < 0) return;
         }
         head = tail;
-        tail = ld_cg(&c->tail);
+        tail = ld_cg(&c->snap[g & 1].tail);
         dprev = dcur;
-        dcur = ld_cg_u64(&c->deg);
+        dcur = ld_cg_u64(&c->snap[g & 1].deg);
         ++level;
+        if (tracer && level <= BFS_TRACE_LEVELS) {
+            c->trace.ns[level] = global_timer_ns() - c->trace.t0;
+            c->trace.tail[level] = tail;
+            c->trace.reads[level] = ld_cg_u64(&c->snap[g & 1].reads);
+        }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) c->levels = level;
+    if (tracer) c->levels = level;
 }
 
 // Levels in the caller's numbering: -1 where the bitmap bit is clear.
@@ -474,6 +527,26 @@ int engine_bfs_plain(DevCtx *c, const GraphPairH &gp, const BfsLayout *L, int32_
         float ms = 0;
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);
         st->gpu_ms = ms;
+    }
+    return FC_OK;
+}
+
+int engine_bfs_trace(DevCtx *c, int32_t *nlevels, int64_t *level_ns, int64_t *frontier,
+                     int64_t *entries, int32_t cap)
+{
+    if (!c->h_bfs_ctr) {
+        *nlevels = 0;
+        return FC_OK;
+    }
+    const BfsCounters *hc = (const BfsCounters *)c->h_bfs_ctr;
+    const int n = std::min(hc->levels, BFS_TRACE_LEVELS);
+    *nlevels = hc->levels;
+    for (int l = 0; l < n && l < cap; ++l) {
+        // level l expands queue [tail[l-1], tail[l]) -- the vertices at distance l
+        const long long b = l == 0 ? 0 : hc->trace.tail[l - 1], e = hc->trace.tail[l];
+        if (level_ns) level_ns[l] = (int64_t)(hc->trace.ns[l + 1] - hc->trace.ns[l]);
+        if (frontier) frontier[l] = e - b;
+        if (entries) entries[l] = (int64_t)(hc->trace.reads[l + 1] - hc->trace.reads[l]);
     }
     return FC_OK;
 }

@@ -130,10 +130,13 @@ __global__ void __launch_bounds__(T, 768 / T) k_persistent(PersistArgs a)
         }
         if (blockIdx.x == 0 && threadIdx.x == 0)
             init_roots(a.mode, gp, s, t, a.status, a.levels, a.log, nv, tc);
-        if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
+        // counters are read from the barrier's snapshot: fast CTAs may
+        // already be claiming for the next step
+        int g = grid_barrier_snap(tc->bar, &tc->err, gridDim.x, SnapTeam{tc});
+        if (g < 0) return;
         if (threadIdx.x == 0)
-            ql_start(ql, a.mode == MODE_STCON, nv, gp.fwd.ne, s, t, ld_cg_u64(&tc->deg[0]),
-                     ld_cg_u64(&tc->deg[1]));
+            ql_start(ql, a.mode == MODE_STCON, nv, gp.fwd.ne, s, t,
+                     ld_cg_u64(&tc->snap[g & 1].deg[0]), ld_cg_u64(&tc->snap[g & 1].deg[1]));
         __syncthreads();
         const int bu_cap = a.mode == MODE_BFS ? 0x7fffffff : LEVEL7_MAX;
         while (true) {
@@ -168,23 +171,26 @@ __global__ void __launch_bounds__(T, 768 / T) k_persistent(PersistArgs a)
                         a.mlp ? &tc->hist[x] : nullptr,
                         TeamSink{a.jobs, a.jcap, &tc->njobs[par], &tc->nok[par]},
                         team_tile_v<T>(F, (long long)(ql.dt[x] - ql.dh[x])));
-            if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
+            g = grid_barrier_snap(tc->bar, &tc->err, gridDim.x, SnapTeam{tc});
+            if (g < 0) return;
             if (ql.dir == DIR_TD) {
                 __shared__ int s_nj;
-                if (threadIdx.x == 0) s_nj = min(ld_cg(&tc->nok[par]), a.jcap);
+                if (threadIdx.x == 0) s_nj = min(ld_cg(&tc->snap[g & 1].nok[par]), a.jcap);
                 __syncthreads();
                 if (s_nj > 0) {  // same value in every CTA: uniform barrier
                     run_team_jobs<T>(a.mode, gp, x, ql.radius[x], a.jobs, s_nj, blockIdx.x,
                                      gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x],
                                      &tc->deg[x], &tc->found, sm, a.mlp ? &tc->hist[x] : nullptr, &tc->inspected);
-                    if (!grid_barrier(tc->bar, &tc->err, gridDim.x)) return;
+                    g = grid_barrier_snap(tc->bar, &tc->err, gridDim.x, SnapTeam{tc});
+                    if (g < 0) return;
                 }
             }
             if (threadIdx.x == 0) {
-                ql_update(ql, ld_cg(&tc->found), ld_cg(&tc->tail[x]), ld_cg_u64(&tc->deg[x]),
-                          ld_cg_u64(&tc->inspected));
+                const TeamSnap &S = tc->snap[g & 1];
+                ql_update(ql, ld_cg(&S.found), ld_cg(&S.tail[x]), ld_cg_u64(&S.deg[x]),
+                          ld_cg_u64(&S.inspected));
                 if (a.mlp) {
-                    ql_update_hist(ql, x, ld_cg_u64(&tc->hist[x]));
+                    ql_update_hist(ql, x, ld_cg_u64(&S.hist[x]));
                 }
             }
             __syncthreads();

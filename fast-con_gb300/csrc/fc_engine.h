@@ -118,6 +118,8 @@ int bfs_layout_build(const GraphPairH &gp, BfsLayout **out, cudaStream_t st, int
 void bfs_layout_free(BfsLayout *L);
 int engine_bfs_plain(DevCtx *c, const GraphPairH &gp, const BfsLayout *L, int32_t s,
                      int32_t *h_levels, fc_stats *st, cudaStream_t stream);
+int engine_bfs_trace(DevCtx *c, int32_t *nlevels, int64_t *level_ns, int64_t *frontier,
+                     int64_t *entries, int32_t cap);
 
 int engine_stcon(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t t, int32_t *conn,
                  int32_t *hops, const fc_opts &o, fc_stats *st, cudaStream_t stream);

@@ -128,17 +128,32 @@ __device__ __forceinline__ void st_release_gpu(int *p, int v)
 constexpr unsigned long long BARRIER_TIMEOUT_NS = 2000000000ull;  // 2 s
 constexpr long long BARRIER_MAX_SPINS = 1ll << 25;
 
-__device__ __forceinline__ bool grid_barrier(int *bar, int *err, int nblocks,
-                                             unsigned long long timeout_ns = BARRIER_TIMEOUT_NS)
+// grid_barrier_snap: the same barrier; in addition the last CTA to arrive
+// calls snap(gen & 1) -- every CTA's writes before the barrier are visible to
+// it -- before it releases the others.  A team whose CTAs read shared
+// counters after a barrier while faster CTAs already update them for the next
+// step reads the snapshot instead: the copy for generation g is rewritten at
+// generation g + 2, after every CTA has passed g + 1.  Returns the generation
+// waited on, or -1 when the wait expired.
+struct NoSnap {
+    __device__ __forceinline__ void operator()(int) const {}
+};
+
+template <class Snap>
+__device__ __forceinline__ int grid_barrier_snap(int *bar, int *err, int nblocks, const Snap &snap,
+                                                 unsigned long long timeout_ns = BARRIER_TIMEOUT_NS)
 {
     __syncthreads();
-    __shared__ int s_ok;
+    __shared__ int s_gen;
     if (threadIdx.x == 0) {
         int ok = 1;
         int gen = ld_acquire_gpu(bar + 1);
         __threadfence();
         int arrived = atomicAdd(bar, 1) + 1;
         if (arrived == nblocks) {
+            __threadfence();
+            snap(gen & 1);
+            __threadfence();
             atomicExch(bar, 0);
             __threadfence();
             st_release_gpu(bar + 1, gen + 1);
@@ -156,10 +171,16 @@ __device__ __forceinline__ bool grid_barrier(int *bar, int *err, int nblocks,
             }
         }
         if (ok && ld_acquire_gpu(err) != 0) ok = 0;
-        s_ok = ok;
+        s_gen = ok ? (gen & 0x7fffffff) : -1;
     }
     __syncthreads();
-    return s_ok != 0;
+    return s_gen;
+}
+
+__device__ __forceinline__ bool grid_barrier(int *bar, int *err, int nblocks,
+                                             unsigned long long timeout_ns = BARRIER_TIMEOUT_NS)
+{
+    return grid_barrier_snap(bar, err, nblocks, NoSnap{}, timeout_ns) >= 0;
 }
 
 }  // namespace fc

@@ -7,6 +7,19 @@
 
 namespace fc {
 
+// The counters a team reads after a step, as they stood when the step's last
+// CTA reached the grid barrier (grid_barrier_snap): faster CTAs may already be
+// adding the next step's claims to the live counters.
+struct TeamSnap {
+    int tail[2];
+    int found;
+    int nok[2];
+    int pad;
+    unsigned long long deg[2];
+    unsigned long long inspected;
+    unsigned long long hist[2];
+};
+
 struct TeamCounters {
     int tail[2];
     int found;
@@ -20,6 +33,23 @@ struct TeamCounters {
                                     // and >= 128 (high 32 bits), learned schedule
     int njobs[2];                   // row-job slots taken, by step parity
     int nok[2];                     // row jobs written (a prefix of the slots)
+    TeamSnap snap[2];               // by barrier generation parity
+};
+
+struct SnapTeam {
+    TeamCounters *tc;
+    __device__ __forceinline__ void operator()(int p) const
+    {
+        TeamSnap &s = tc->snap[p];
+        for (int x = 0; x < 2; ++x) {
+            s.tail[x] = ld_cg(&tc->tail[x]);
+            s.nok[x] = ld_cg(&tc->nok[x]);
+            s.deg[x] = ld_cg_u64(&tc->deg[x]);
+            s.hist[x] = ld_cg_u64(&tc->hist[x]);
+        }
+        s.found = ld_cg(&tc->found);
+        s.inspected = ld_cg_u64(&tc->inspected);
+    }
 };
 
 // degree bins of the frontier histogram: < 8, < 128, >= 128; the counters

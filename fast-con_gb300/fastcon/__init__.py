@@ -37,6 +37,7 @@ EXPORTS = [
     "fc_opts_init", "fc_graph_load_edgelist", "fc_graph_from_csr", "fc_graph_from_edges",
     "fc_graph_from_device_edges", "fc_graph_generate_rmat", "fc_graph_generate_grid",
     "fc_graph_info", "fc_graph_get_csr", "fc_graph_free", "fc_bfs_levels", "fc_bfs_levels_ex",
+    "fc_bfs_trace",
     "fc_stcon", "fc_stcon_ex", "fc_stcon_depth", "fc_stcon_batch", "fc_stcon_batch_device",
     "fc_stcon_batch_noalloc", "fc_sched_set_weights", "fc_sched_get_weights",
     "fc_mlp_loss_grad", "fc_mlp_train", "fc_stcon_batch_scripted", "fc_selftest_wait",
@@ -416,6 +417,18 @@ def selftest_wait(timeout_ms: int = 200):
     ms = np.zeros(1, np.float64)
     rc = lib().fc_selftest_wait(int(timeout_ms), _P(ms))
     return rc, float(ms[0])
+
+
+def bfs_trace(cap: int = 256):
+    """Per-level trace of the last plain-BFS-engine search on this device:
+    dict of level_ns, frontier, entries (numpy int64 arrays)."""
+    n = ctypes.c_int32()
+    ns = np.zeros(cap, np.int64)
+    fr = np.zeros(cap, np.int64)
+    en = np.zeros(cap, np.int64)
+    _check(lib().fc_bfs_trace(ctypes.byref(n), _P(ns), _P(fr), _P(en), int(cap)), "fc_bfs_trace")
+    k = min(n.value, cap)
+    return {"levels": n.value, "level_ns": ns[:k], "frontier": fr[:k], "entries": en[:k]}
 
 
 def device_info():

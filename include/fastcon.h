@@ -196,6 +196,15 @@ int fc_bfs_levels(fc_graph *g, int32_t s, int32_t *levels);
 int fc_bfs_levels_ex(fc_graph *g, int32_t s, int32_t *levels, const fc_opts *opts,
                      fc_stats *stats);
 
+/* Per-level record of the last plain-BFS-engine search on the current device
+ * (the reference times its levels under DBG_TIME, START_TIMER / STOP_TIMER in
+ * S/include/header.h): *nlevels = levels expanded; for the first min(cap,
+ * 256) levels l (nullable arrays): level_ns[l] = device time of level l's
+ * expansion, frontier[l] = vertices at distance l, entries[l] = adjacency
+ * entries read expanding them. */
+int fc_bfs_trace(int32_t *nlevels, int64_t *level_ns, int64_t *frontier, int64_t *entries,
+                 int32_t cap);
+
 /* One s-t connectivity query: connected flag and exact hop distance (-1 when
  * not connected).  Replaces make_stcon (S/include/make_stcon.h:11-17,
  * S/make_stcon.c:730-1497), which returns only DEPTH = ceil(d/2), and the
