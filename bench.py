@@ -692,7 +692,8 @@ def run_bfs(args, cfg):
                      engine={"hostloop": fc.ENGINE_HOSTLOOP, "persistent": fc.ENGINE_PERSISTENT,
                              "auto": fc.ENGINE_AUTO}[args.engine],
                      vertex_order={"auto": fc.ORDER_AUTO, "given": fc.ORDER_GIVEN,
-                                   "degree": fc.ORDER_DEGREE}[args.order])
+                                   "degree": fc.ORDER_DEGREE}[args.order],
+                     ctas_per_sm=args.ctas)
     ms = []
     for k in range(args.warmup + args.steps):
         lev, st = G.bfs_levels(src, o, stats=True)
@@ -705,7 +706,8 @@ def run_bfs(args, cfg):
         tr = fc.bfs_trace()
         trace = {"level_us": (tr["level_ns"] / 1e3).round(1).tolist(),
                  "frontier": tr["frontier"].tolist(), "entries": tr["entries"].tolist()}
-    print(json.dumps({"bfs": args.bfs, "engine": args.engine, "order": args.order, "trace": trace,
+    print(json.dumps({"bfs": args.bfs, "engine": args.engine, "order": args.order,
+                      "ctas": args.ctas, "trace": trace,
                       "workload": args.config,
                       "source": src, "levels": np.bincount(lev[reached]).tolist(),
                       "ms": min(ms), "entries_inspected": int(st["edges_inspected"]),
@@ -726,6 +728,8 @@ def main():
                     help="engine of --bfs (auto: the plain BFS engine for --bfs plain)")
     ap.add_argument("--order", default="auto", choices=["auto", "given", "degree"],
                     help="vertex numbering of the plain BFS engine (--bfs plain --engine auto)")
+    ap.add_argument("--ctas", type=int, default=0,
+                    help="resident CTAs per SM of the plain BFS engine (2, 3 or 4; 0 = default)")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     import oracle

@@ -446,7 +446,8 @@ int fc_bfs_levels_ex(fc_graph *g, int32_t s, int32_t *levels, const fc_opts *opt
             }
             lay = g->bfs_layout;
         }
-        return fc::engine_bfs_plain(L.c, pair_of(g), lay, s, levels, stats, pick_stream(opts, L.c));
+        return fc::engine_bfs_plain(L.c, pair_of(g), lay, s, levels, o, stats,
+                                    pick_stream(opts, L.c));
     }
     return fc::engine_bfs(L.c, pair_of(g), s, levels, o, stats, pick_stream(opts, L.c));
 }

@@ -25,10 +25,14 @@
 //   levels are mapped back to the caller's numbering in the output pass.
 //   Levels do not depend on the numbering.
 //
-// Work per level: the frontier is the level's range of the visit queue; it is
-// cut into tiles of frontier vertices sized by their degree sum and expanded
-// by load-balanced search (fc_step.cuh), rows longer than TEAM_SPLIT_E
-// entries being cut into row jobs that the whole grid walks after the tiles.
+// Work per level, with no CTA barrier: each warp takes work from the level's
+// queues on its own (its first item by its index, later ones from an atomic
+// counter).  Long rows come as pieces of at most BFS_PIECE entries, walked
+// with 16-byte column loads; short rows come 32 * V to a chunk, laid end to
+// end by a warp prefix sum and read by load-balanced search within the warp
+// (after Merrill, Garland & Grimshaw, PPoPP 2012).  Claims gather in a
+// per-warp shared-memory buffer and reach the next level's queues with one
+// reservation per buffer.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -255,53 +259,76 @@ int bfs_layout_build(const GraphPairH &gp, BfsLayout **out, cudaStream_t st, int
 // ---------------------------------------------------------------------------
 // the search
 // ---------------------------------------------------------------------------
-struct BfsSnap {  // counters as they stood at a level's last barrier
-    int tail;
-    int nok[2];
-    int pad;
-    unsigned long long deg;
-    unsigned long long reads;
+// Frontier queues, by the parity of the level they hold.  A claimed vertex
+// goes, with its row range, to the short queue (1..BFS_MED entries) or, cut
+// into pieces of at most BFS_PIECE entries, to the piece queue; vertices
+// without neighbours are not queued.  A level reads its queues with no row
+// lookup: the claimer already read the row range.
+constexpr int BFS_T = 256;
+constexpr int BFS_MED = 256;      // longer rows are walked in pieces
+constexpr int BFS_PIECE = 2048;   // entries per piece
+constexpr int BFS_VMAX = 4;       // short-queue vertices per lane in one chunk
+constexpr int BFS_KMAX = 16;      // entries per lane and round, at most
+constexpr int BFS_WLOG = 32 * BFS_KMAX;  // claims buffered per warp (one round's worth)
+
+struct BfsSnap {  // the next frontier's counters as they stood at the level's last barrier
+    unsigned long long qc;   // (short vertices << 32) | pieces
+    unsigned long long qds;  // adjacency entries of the short vertices
+    unsigned long long qdl;  // (other claimed vertices << 40) | entries of the long ones
+    unsigned long long pad;
 };
 
 // Per-level record of the last search (the first BFS_TRACE_LEVELS levels):
-// start time from %globaltimer, frontier end in the queue, entries read before
-// the level.  The reference times its levels under DBG_TIME (START_TIMER /
+// start time from %globaltimer, vertices and adjacency entries of the
+// frontier.  The reference times its levels under DBG_TIME (START_TIMER /
 // STOP_TIMER, S/include/header.h).
 constexpr int BFS_TRACE_LEVELS = 256;
 struct BfsTrace {
     unsigned long long t0;
     unsigned long long ns[BFS_TRACE_LEVELS + 1];
-    long long tail[BFS_TRACE_LEVELS + 1];
-    unsigned long long reads[BFS_TRACE_LEVELS + 1];
+    long long frontier[BFS_TRACE_LEVELS + 1];
+    unsigned long long entries[BFS_TRACE_LEVELS + 1];
+};
+
+// Counters in separate 128-byte lines: the flush reservations, the dynamic
+// fetches and the barrier words (polled by every waiting CTA) do not share
+// a line, so waiting CTAs do not queue behind the working ones' atomics.
+struct alignas(128) BfsQueueCtr {
+    unsigned long long qc[2];     // live counters of the queue pair being filled, by parity
+    unsigned long long qds[2];
+    unsigned long long qdl[2];
+};
+struct alignas(128) BfsFetchCtr {
+    int fetch_s[2], fetch_p[2];   // dynamic batches taken, by level parity
+};
+struct alignas(128) BfsBarrier {
+    int bar[2];
+    int err;
 };
 
 struct BfsCounters {
-    int tail;   // vertices queued (= reached)
-    int err;
-    int bar[2];
-    int njobs[2];
-    int nok[2];
-    unsigned long long deg;    // degree sum of the queued vertices
-    unsigned long long reads;  // adjacency entries read
-    unsigned long long root_deg;
-    int levels;                // levels expanded
+    BfsQueueCtr q;
+    BfsFetchCtr f;
+    BfsBarrier b;
+    int levels;                   // levels expanded
     int pad;
-    BfsSnap snap[2];           // by barrier generation parity
+    unsigned long long init_qc, init_qds, init_qdl;  // the root's queues
+    long long overflow;           // queue writes refused (never, by construction)
+    unsigned long long reached;   // vertices at some distance (totals, kept by the tracer)
+    unsigned long long entries;   // adjacency entries of those vertices = entries read
+    BfsSnap snap[2];              // by barrier generation parity
     BfsTrace trace;
 };
 
-// Every CTA reads the level's counters from the barrier's snapshot: the
-// fastest CTAs are already claiming the next level's vertices.
 struct SnapBfs {
     BfsCounters *c;
+    int np;  // parity of the queues the level filled
     __device__ __forceinline__ void operator()(int p) const
     {
         BfsSnap &s = c->snap[p];
-        s.tail = ld_cg(&c->tail);
-        s.nok[0] = ld_cg(&c->nok[0]);
-        s.nok[1] = ld_cg(&c->nok[1]);
-        s.deg = ld_cg_u64(&c->deg);
-        s.reads = ld_cg_u64(&c->reads);
+        s.qc = ld_cg_u64(&c->q.qc[np]);
+        s.qds = ld_cg_u64(&c->q.qds[np]);
+        s.qdl = ld_cg_u64(&c->q.qdl[np]);
     }
 };
 
@@ -332,14 +359,220 @@ struct BfsArgs {
     int nv;
     unsigned *bm;
     int32_t *lev;
-    int32_t *queue;
+    int2 *sq[2];       // short queues
+    int2 *pq[2];       // piece queues
+    long long scap, pcap;
     BfsCounters *ctr;
-    int2 *jobs;
-    int jcap;
 };
 
-constexpr int BFS_T = 256;
-constexpr int BFS_MIN_CTAS = 4;  // resident CTAs per SM the register budget allows
+struct BfsWarpSmem {
+    int off[32 * BFS_VMAX + 1];  // chunk rows laid end to end
+    int rbs[32 * BFS_VMAX];      // and their first entries
+    int buf[BFS_WLOG];           // claimed vertices not yet queued
+    int cnt;
+};
+
+// Move the warp's buffered claims into the next frontier's queues: one
+// reservation per counter for the whole buffer.  Lane l owns buffer entries
+// l, l + 32, ...; their row ranges are read eight at a time (loads in
+// flight together) to count, then read again -- from the cache -- to write.
+constexpr int BFS_FLUSH_ILP = 8;
+__device__ __noinline__ void bfs_flush(const BfsArgs &a, BfsWarpSmem &w, int np)
+{
+    const int lane = (int)lane_id();
+    const int n = w.cnt;
+    if (n == 0) return;
+    int ns = 0, npc = 0, nother = 0;
+    long long dsh = 0, dlo = 0;
+    for (int i0 = 0; i0 < n; i0 += 32 * BFS_FLUSH_ILP) {
+        int v[BFS_FLUSH_ILP], d[BFS_FLUSH_ILP];
+#pragma unroll
+        for (int j = 0; j < BFS_FLUSH_ILP; ++j) {
+            const int i = i0 + j * 32 + lane;
+            v[j] = i < n ? w.buf[i] : -1;
+        }
+#pragma unroll
+        for (int j = 0; j < BFS_FLUSH_ILP; ++j)
+            d[j] = v[j] >= 0 ? __ldg(a.row_ptr + v[j] + 1) - __ldg(a.row_ptr + v[j]) : -1;
+#pragma unroll
+        for (int j = 0; j < BFS_FLUSH_ILP; ++j) {
+            if (d[j] < 0) continue;
+            if (d[j] > 0 && d[j] <= BFS_MED) {
+                ++ns;
+                dsh += d[j];
+            } else {
+                ++nother;
+                if (d[j] > 0) {
+                    npc += (d[j] + BFS_PIECE - 1) / BFS_PIECE;
+                    dlo += d[j];
+                }
+            }
+        }
+    }
+    const int s_incl = warp_inclusive_scan(ns), p_incl = warp_inclusive_scan(npc);
+    const int s_tot = __shfl_sync(0xffffffffu, s_incl, 31);
+    const int p_tot = __shfl_sync(0xffffffffu, p_incl, 31);
+    dsh = warp_sum_ll(dsh);
+    dlo = warp_sum_ll(dlo);
+    nother = warp_sum_i(nother);
+    unsigned long long base = 0;
+    BfsCounters *c = a.ctr;
+    if (lane == 0) {
+        base = atomicAdd(&c->q.qc[np], ((unsigned long long)s_tot << 32) | (unsigned)p_tot);
+        if (dsh) atomicAdd(&c->q.qds[np], (unsigned long long)dsh);
+        if (nother)
+            atomicAdd(&c->q.qdl[np], ((unsigned long long)nother << 40) | (unsigned long long)dlo);
+    }
+    base = __shfl_sync(0xffffffffu, base, 0);
+    long long sb = (long long)(base >> 32) + s_incl - ns;
+    long long pb = (long long)(base & 0xffffffffu) + p_incl - npc;
+    int2 *sq = a.sq[np], *pq = a.pq[np];
+    int refused = 0;
+    for (int i0 = 0; i0 < n; i0 += 32 * BFS_FLUSH_ILP) {
+        int v[BFS_FLUSH_ILP], b[BFS_FLUSH_ILP], e[BFS_FLUSH_ILP];
+#pragma unroll
+        for (int j = 0; j < BFS_FLUSH_ILP; ++j) {
+            const int i = i0 + j * 32 + lane;
+            v[j] = i < n ? w.buf[i] : -1;
+        }
+#pragma unroll
+        for (int j = 0; j < BFS_FLUSH_ILP; ++j) {
+            b[j] = v[j] >= 0 ? __ldg(a.row_ptr + v[j]) : 0;
+            e[j] = v[j] >= 0 ? __ldg(a.row_ptr + v[j] + 1) : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < BFS_FLUSH_ILP; ++j) {
+            const int d = e[j] - b[j];
+            if (d > 0 && d <= BFS_MED) {
+                if (sb < a.scap) sq[sb] = make_int2(b[j], e[j]);
+                else ++refused;
+                ++sb;
+            } else if (d > 0) {
+                for (int x = b[j]; x < e[j]; x += BFS_PIECE) {
+                    if (pb < a.pcap) pq[pb] = make_int2(x, min(e[j], x + BFS_PIECE));
+                    else ++refused;
+                    ++pb;
+                }
+            }
+        }
+    }
+    refused = warp_sum_i(refused);
+    if (lane == 0 && refused) atomicAdd((unsigned long long *)&c->overflow, (unsigned long long)refused);
+    __syncwarp();
+    if (lane == 0) w.cnt = 0;
+    __syncwarp();
+}
+
+// Buffer the claims of one round (c[k] = claimed vertex or -1); the buffer
+// holds one full round, so it is flushed first when the round would not fit.
+template <int K>
+__device__ __forceinline__ void bfs_append(const BfsArgs &a, BfsWarpSmem &w, const int (&c)[K],
+                                           int np)
+{
+    int cnt = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) cnt += c[k] >= 0;
+    if (!__any_sync(0xffffffffu, cnt > 0)) return;
+    const int incl = warp_inclusive_scan(cnt);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int n0 = w.cnt;
+    if (n0 + total > BFS_WLOG) {
+        bfs_flush(a, w, np);
+        n0 = 0;
+    }
+    int pos = n0 + incl - cnt;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        if (c[k] >= 0) w.buf[pos++] = c[k];
+    __syncwarp();
+    if (lane_id() == 0) w.cnt = n0 + total;
+    __syncwarp();
+}
+
+// A piece of one long row: P 16-byte column loads per lane and round
+// (128 P entries), the unaligned ends with scalar loads.
+template <int P>
+__device__ __noinline__ void bfs_piece(const BfsArgs &a, BfsWarpSmem &w, int2 pc,
+                                       VisitBitmap vis, int np)
+{
+    const int lane = (int)lane_id();
+    const int b = pc.x, e = pc.y;
+    const int al = min((b + 3) & ~3, e);
+    const int z = max(e & ~3, al);
+    const int nhead = al - b, ntail = e - z;
+    if (nhead + ntail > 0) {
+        int c[1] = {-1};
+        if (lane < nhead)
+            c[0] = vis.visit(__ldg(a.col + b + lane));
+        else if (lane < nhead + ntail)
+            c[0] = vis.visit(__ldg(a.col + z + lane - nhead));
+        bfs_append<1>(a, w, c, np);
+    }
+    const int4 *col4 = reinterpret_cast<const int4 *>(a.col);
+    const int k_end = z >> 2;
+    for (int k0 = al >> 2; k0 < k_end; k0 += P * 32) {
+        int v[4 * P], c[4 * P];
+#pragma unroll
+        for (int h = 0; h < P; ++h) {
+            const int k = k0 + h * 32 + lane;
+            int4 x = make_int4(-1, -1, -1, -1);
+            if (k < k_end) x = __ldg(col4 + k);
+            v[4 * h + 0] = x.x;
+            v[4 * h + 1] = x.y;
+            v[4 * h + 2] = x.z;
+            v[4 * h + 3] = x.w;
+        }
+        visit_k<4 * P>(vis, v, c);
+        bfs_append<4 * P>(a, w, c, np);
+    }
+}
+
+// A chunk of 32 * V short-queue vertices: their rows laid end to end in the
+// warp's shared memory, K entries per lane and round, each entry's row found
+// by binary search over the chunk's prefix (load-balanced search within one
+// warp: no CTA barrier).
+template <int V, int K>
+__device__ __noinline__ void bfs_chunk(const BfsArgs &a, BfsWarpSmem &w, const int2 *sq, int Fs,
+                                       int first, VisitBitmap vis, int np)
+{
+    const int lane = (int)lane_id();
+    int2 r[V];
+    int sum = 0;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        const int i = first + lane * V + v;
+        r[v] = i < Fs ? sq[i] : make_int2(0, 0);
+        sum += r[v].y - r[v].x;
+    }
+    const int incl = warp_inclusive_scan(sum);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int run = incl - sum;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        w.off[lane * V + v] = run;
+        w.rbs[lane * V + v] = r[v].x;
+        run += r[v].y - r[v].x;
+    }
+    __syncwarp();
+    for (int base = 0; base < total; base += 32 * K) {
+        int v[K], c[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const int e = base + j * 32 + lane;
+            v[j] = -1;
+            if (e < total) {
+                int lo = 0;  // the last row starting at or before e
+#pragma unroll
+                for (int s = 16 * V; s > 0; s >>= 1)  // lo + s stays below 32 * V
+                    if (w.off[lo + s] <= e) lo += s;
+                v[j] = __ldg(a.col + w.rbs[lo] + (e - w.off[lo]));
+            }
+        }
+        visit_k<K>(vis, v, c);
+        bfs_append<K>(a, w, c, np);
+    }
+    __syncwarp();  // off / rbs are rewritten by the next chunk
+}
 
 __global__ void k_bfs_root(BfsArgs a, int s)
 {
@@ -347,66 +580,115 @@ __global__ void k_bfs_root(BfsArgs a, int s)
     BfsCounters *c = a.ctr;
     a.bm[s >> 5] |= 1u << (s & 31);
     a.lev[s] = 0;
-    a.queue[0] = s;
-    c->tail = 1;
-    c->err = 0;
-    c->njobs[0] = c->njobs[1] = 0;
-    c->nok[0] = c->nok[1] = 0;
-    c->deg = (unsigned long long)(a.row_ptr[s + 1] - a.row_ptr[s]);
-    c->root_deg = c->deg;
-    c->reads = 0;
+    const int b = a.row_ptr[s], e = a.row_ptr[s + 1], d = e - b;
+    unsigned long long ns = 0, np = 0, other = 1;
+    if (d > 0 && d <= BFS_MED) {
+        a.sq[0][0] = make_int2(b, e);
+        ns = 1;
+        other = 0;
+    } else {
+        for (int x = b; x < e; x += BFS_PIECE) a.pq[0][np++] = make_int2(x, min(e, x + BFS_PIECE));
+    }
+    c->init_qc = (ns << 32) | np;
+    c->init_qds = ns ? (unsigned long long)d : 0;
+    c->init_qdl = (other << 40) | (ns ? 0ull : (unsigned long long)d);
+    for (int p = 0; p < 2; ++p) {
+        c->q.qc[p] = c->q.qds[p] = c->q.qdl[p] = 0;
+        c->f.fetch_s[p] = c->f.fetch_p[p] = 0;
+    }
+    c->b.err = 0;
     c->levels = 0;
-    c->bar[0] = 0;  // arrivals (a launch that gave up at a barrier may have left some)
+    c->overflow = 0;
+    c->reached = 0;
+    c->entries = 0;
+    c->b.bar[0] = 0;  // arrivals (a launch that gave up at a barrier may have left some)
 }
 
-template <int T>
-__global__ void __launch_bounds__(T, BFS_MIN_CTAS) k_bfs_plain(BfsArgs a)
+// MINB resident CTAs per SM (the register budget) and K entries per lane and
+// round go together: 4 x 8 (64 registers), 3 x 8 (80), 2 x 16 (128).  On
+// R-MAT 24 the three measure within run-to-run noise of each other (1.5-1.9
+// ms); more entries per round, a software-pipelined round (the next round's
+// column loads issued before this round's probes) and a shared-memory copy
+// of the hubs' bitmap words each measured no faster.
+template <int T, int MINB, int K>
+__global__ void __launch_bounds__(T, MINB) k_bfs_plain(BfsArgs args)
 {
-    __shared__ SmemTopDown<T> sm;
-    __shared__ int s_nj;
-    BfsCounters *c = a.ctr;
-    int head = 0, tail = 1, level = 0;
-    unsigned long long dprev = 0, dcur = ld_cg_u64(&c->root_deg);
+    __shared__ BfsWarpSmem wsm[T / 32];
+    __shared__ BfsArgs a;  // the helpers read the arguments from shared memory
+    if (threadIdx.x == 0) a = args;
+    __syncthreads();
+    BfsCounters *c = args.ctr;
+    const int lane = (int)lane_id();
+    BfsWarpSmem &w = wsm[threadIdx.x >> 5];
+    if (lane == 0) w.cnt = 0;
+    __syncwarp();
+    const int gw = (int)((blockIdx.x * T + threadIdx.x) >> 5);
+    const int nw = (int)(gridDim.x * (T / 32));
+    unsigned long long qc = ld_cg_u64(&c->init_qc), qds = ld_cg_u64(&c->init_qds),
+                       qdl = ld_cg_u64(&c->init_qdl);
     const bool tracer = blockIdx.x == 0 && threadIdx.x == 0;
-    if (tracer) {
-        c->trace.t0 = global_timer_ns();
-        c->trace.ns[0] = 0;
-        c->trace.tail[0] = 1;
-        c->trace.reads[0] = 0;
-    }
-    while (tail > head) {
-        const int F = tail - head;
-        const int par = level & 1;
-        // the other parity's job counters were last read before the previous
-        // level's final barrier: clearing them cannot race
+    if (tracer) c->trace.t0 = global_timer_ns();
+    int level = 0;
+    while (true) {
+        const int Fs = (int)(qc >> 32), Fp = (int)(qc & 0xffffffffu);
+        const long long fr = (long long)Fs + (long long)(qdl >> 40);  // vertices at this distance
+        if (tracer) {
+            const unsigned long long en = qds + (qdl & ((1ull << 40) - 1));
+            c->reached += (unsigned long long)fr;
+            c->entries += en;
+            if (level <= BFS_TRACE_LEVELS) {
+                c->trace.ns[level] = global_timer_ns() - c->trace.t0;
+                c->trace.frontier[level] = fr;
+                c->trace.entries[level] = en;
+            }
+        }
+        if (Fs == 0 && Fp == 0) {
+            // a level of vertices without out-edges still counts as a level
+            if (fr > 0) ++level;
+            break;
+        }
+        const int p = level & 1, np = p ^ 1;
+        // the live counters of parity p described this level's queues; every
+        // CTA took them from the last barrier's snapshot, and the next level
+        // refills them.  The other parity's fetch counters were last used a
+        // level ago, before the last barrier.
         if (blockIdx.x == 0 && threadIdx.x == 0) {
-            c->njobs[par ^ 1] = 0;
-            c->nok[par ^ 1] = 0;
+            c->q.qc[p] = c->q.qds[p] = c->q.qdl[p] = 0;
+            c->f.fetch_s[np] = c->f.fetch_p[np] = 0;
         }
-        const VisitBitmap vis{a.bm, a.lev, level + 1};
-        const AppendTarget app{a.queue, a.nv, 0, &c->tail, &c->deg, a.row_ptr, nullptr, &c->reads};
-        topdown_step<T>(a.row_ptr, a.col, a.queue + head, F, blockIdx.x, gridDim.x, vis, app, sm,
-                        nullptr, TeamSink{a.jobs, a.jcap, &c->njobs[par], &c->nok[par]},
-                        team_tile_v<T>(F, (long long)(dcur - dprev)));
-        int g = grid_barrier_snap(c->bar, &c->err, gridDim.x, SnapBfs{c});
+        const VisitBitmap vis{args.bm, args.lev, level + 1};
+        // pieces: batch gw first without a fetch, later ones from the counter
+        for (int i = gw; i < Fp;) {
+            bfs_piece<K / 4>(a, w, args.pq[p][i], vis, np);
+            int k = 0;
+            if (lane == 0) k = atomicAdd(&c->f.fetch_p[p], 1);
+            i = nw + __shfl_sync(0xffffffffu, k, 0);
+        }
+        // short vertices: chunks of 32 * V, V by the frontier's mean degree
+        if (Fs > 0) {
+            const long long avg = (long long)(qds / (unsigned long long)Fs);
+            const int V = (avg >= 16 || Fs < 32 * 2 * nw) ? 1 : ((avg >= 6 || Fs < 32 * 4 * nw) ? 2 : 4);
+            const int cw = 32 * V;
+            const int nch = (Fs + cw - 1) / cw;
+            for (int i = gw; i < nch;) {
+                if (V == 1)
+                    bfs_chunk<1, K>(a, w, args.sq[p], Fs, i * cw, vis, np);
+                else if (V == 2)
+                    bfs_chunk<2, K>(a, w, args.sq[p], Fs, i * cw, vis, np);
+                else
+                    bfs_chunk<4, K>(a, w, args.sq[p], Fs, i * cw, vis, np);
+                int k = 0;
+                if (lane == 0) k = atomicAdd(&c->f.fetch_s[p], 1);
+                i = nw + __shfl_sync(0xffffffffu, k, 0);
+            }
+        }
+        bfs_flush(a, w, np);
+        const int g = grid_barrier_snap(c->b.bar, &c->b.err, gridDim.x, SnapBfs{c, np});
         if (g < 0) return;
-        if (threadIdx.x == 0) s_nj = min(ld_cg(&c->snap[g & 1].nok[par]), a.jcap);
-        __syncthreads();
-        if (s_nj > 0) {  // the same value in every CTA: a uniform barrier
-            team_jobs<T>(a.col, a.jobs, s_nj, blockIdx.x, gridDim.x, vis, app, sm, nullptr);
-            g = grid_barrier_snap(c->bar, &c->err, gridDim.x, SnapBfs{c});
-            if (g < 0) return;
-        }
-        head = tail;
-        tail = ld_cg(&c->snap[g & 1].tail);
-        dprev = dcur;
-        dcur = ld_cg_u64(&c->snap[g & 1].deg);
+        qc = ld_cg_u64(&c->snap[g & 1].qc);
+        qds = ld_cg_u64(&c->snap[g & 1].qds);
+        qdl = ld_cg_u64(&c->snap[g & 1].qdl);
         ++level;
-        if (tracer && level <= BFS_TRACE_LEVELS) {
-            c->trace.ns[level] = global_timer_ns() - c->trace.t0;
-            c->trace.tail[level] = tail;
-            c->trace.reads[level] = ld_cg_u64(&c->snap[g & 1].reads);
-        }
     }
     if (tracer) c->levels = level;
 }
@@ -423,55 +705,62 @@ __global__ void k_bfs_out(const unsigned *bm, const int32_t *lev, const int32_t 
     }
 }
 
-static int ensure_bfs_ws(DevCtx *c, size_t nv)
+static int ensure_bfs_ws(DevCtx *c, size_t nv, long long ne)
 {
     if (!c->bfs_ctr) {
         FC_CUDA_TRY(cudaMalloc(&c->bfs_ctr, sizeof(BfsCounters)));
         FC_CUDA_TRY(cudaMemset(c->bfs_ctr, 0, sizeof(BfsCounters)));
         FC_CUDA_TRY(cudaMallocHost(&c->h_bfs_ctr, sizeof(BfsCounters)));
-        // 2^20 jobs of TEAM_SPLIT_E entries: any level of a graph of up to 2^32 entries
-        FC_CUDA_TRY(cudaMalloc(&c->bfs_jobs, sizeof(int2) << 20));
-        c->bfs_jcap = 1 << 20;
+        std::memset(c->h_bfs_ctr, 0, sizeof(BfsCounters));
     }
-    if (c->bfs_nv >= nv && c->bfs_bm) return FC_OK;
+    // pieces: at most one per long row plus one per BFS_PIECE entries
+    const long long pcap = (long long)nv + ne / BFS_PIECE + 2;
+    if (c->bfs_nv >= nv && c->bfs_pcap >= pcap && c->bfs_bm) return FC_OK;
     cudaFree(c->bfs_bm);
     cudaFree(c->bfs_lev);
-    cudaFree(c->bfs_q);
     cudaFree(c->bfs_out);
+    cudaFree(c->bfs_q);
     c->bfs_bm = nullptr;
-    c->bfs_lev = c->bfs_q = c->bfs_out = nullptr;
+    c->bfs_lev = c->bfs_out = nullptr;
+    c->bfs_q = nullptr;
     c->bfs_nv = 0;
+    c->bfs_pcap = 0;
     const size_t words = (nv + 1023) / 1024 * 32;  // whole 128-byte lines
     FC_CUDA_TRY(cudaMalloc(&c->bfs_bm, words * sizeof(unsigned)));
     FC_CUDA_TRY(cudaMalloc(&c->bfs_lev, nv * sizeof(int32_t)));
-    FC_CUDA_TRY(cudaMalloc(&c->bfs_q, nv * sizeof(int32_t)));
     FC_CUDA_TRY(cudaMalloc(&c->bfs_out, nv * sizeof(int32_t)));
+    // two short queues of nv ranges and two piece queues of pcap ranges
+    FC_CUDA_TRY(cudaMalloc(&c->bfs_q, sizeof(int2) * (2 * nv + 2 * (size_t)pcap)));
     FC_CUDA_TRY(cudaDeviceSynchronize());
     c->bfs_nv = nv;
+    c->bfs_pcap = pcap;
     return FC_OK;
 }
 
-static int bfs_grid(DevCtx *c)
+static int bfs_grid(DevCtx *c, const void *fn)
 {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bfs_plain<BFS_T>, BFS_T, 0) !=
-            cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BFS_T, 0) != cudaSuccess ||
         per_sm < 1)
         return 0;
     return per_sm * c->sm_count;
 }
 
 int engine_bfs_plain(DevCtx *c, const GraphPairH &gp, const BfsLayout *L, int32_t s,
-                     int32_t *h_levels, fc_stats *st, cudaStream_t stream)
+                     int32_t *h_levels, const fc_opts &o, fc_stats *st, cudaStream_t stream)
 {
     const int nv = gp.fwd.nv;
-    int rc = ensure_bfs_ws(c, (size_t)nv);
+    int rc = ensure_bfs_ws(c, (size_t)nv, gp.fwd.ne);
     if (rc) return rc;
     if (!c->coop) {
         set_error("cooperative launch not supported on this device");
         return FC_ERR_UNSUPPORTED;
     }
-    const int grid = bfs_grid(c);
+    // resident CTAs per SM (fc_opts.ctas_per_sm): 2, 3 or 4 (the default)
+    const void *fn = o.ctas_per_sm == 2   ? (const void *)k_bfs_plain<BFS_T, 2, 16>
+                     : o.ctas_per_sm == 3 ? (const void *)k_bfs_plain<BFS_T, 3, 8>
+                                          : (const void *)k_bfs_plain<BFS_T, 4, 8>;
+    const int grid = bfs_grid(c, fn);
     if (grid < 1) {
         set_error("k_bfs_plain cannot be resident");
         return FC_ERR_CUDA;
@@ -482,10 +771,13 @@ int engine_bfs_plain(DevCtx *c, const GraphPairH &gp, const BfsLayout *L, int32_
     a.nv = nv;
     a.bm = c->bfs_bm;
     a.lev = c->bfs_lev;
-    a.queue = c->bfs_q;
+    a.scap = nv;
+    a.pcap = c->bfs_pcap;
+    a.sq[0] = c->bfs_q;
+    a.sq[1] = c->bfs_q + nv;
+    a.pq[0] = c->bfs_q + 2 * (size_t)nv;
+    a.pq[1] = a.pq[0] + c->bfs_pcap;
     a.ctr = (BfsCounters *)c->bfs_ctr;
-    a.jobs = c->bfs_jobs;
-    a.jcap = c->bfs_jcap;
     // the root in the search's numbering (one element read back)
     int32_t root = s;
     if (L)
@@ -497,8 +789,7 @@ int engine_bfs_plain(DevCtx *c, const GraphPairH &gp, const BfsLayout *L, int32_
     k_bfs_root<<<1, 32, 0, stream>>>(a, root);
     FC_CUDA_TRY(cudaGetLastError());
     void *args[] = {&a};
-    FC_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_bfs_plain<BFS_T>, dim3(grid),
-                                            dim3(BFS_T), args, 0, stream));
+    FC_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(BFS_T), args, 0, stream));
     const int ogrid = (int)std::min<long long>(8 * (long long)c->sm_count, ((long long)nv + 255) / 256);
     k_bfs_out<<<ogrid, 256, 0, stream>>>(a.bm, a.lev, L ? L->new_id : nullptr, nv, c->bfs_out);
     FC_CUDA_TRY(cudaGetLastError());
@@ -510,20 +801,24 @@ int engine_bfs_plain(DevCtx *c, const GraphPairH &gp, const BfsLayout *L, int32_
                                     cudaMemcpyDeviceToHost, stream));
     FC_CUDA_TRY(cudaStreamSynchronize(stream));
     const BfsCounters *hc = (const BfsCounters *)c->h_bfs_ctr;
-    if (hc->err) {
+    if (hc->b.err) {
         set_error("k_bfs_plain: a grid barrier wait expired");
         return FC_ERR_TIMEOUT;
     }
+    if (hc->overflow) {
+        set_error("k_bfs_plain: %lld frontier queue writes refused", (long long)hc->overflow);
+        return FC_ERR_CUDA;
+    }
     if (st) {
         std::memset(st, 0, sizeof(*st));
-        const long long reached = hc->tail;
-        st->edges_inspected = (int64_t)hc->reads;
+        const long long reached = (long long)hc->reached;
+        st->edges_inspected = (int64_t)hc->entries;
         st->visited = reached;
         st->steps = hc->levels;
         // 12 per frontier vertex + 8 per entry read + 8 per claimed vertex
-        st->alg_bytes = (int64_t)(12 * reached + 8 * (long long)hc->reads + 8 * (reached - 1));
+        st->alg_bytes = (int64_t)(12 * reached + 8 * (long long)hc->entries + 8 * (reached - 1));
         st->launches = 4;
-        st->visited_adjacency = (int64_t)hc->deg;
+        st->visited_adjacency = (int64_t)hc->entries;
         float ms = 0;
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);
         st->gpu_ms = ms;
@@ -539,14 +834,12 @@ int engine_bfs_trace(DevCtx *c, int32_t *nlevels, int64_t *level_ns, int64_t *fr
         return FC_OK;
     }
     const BfsCounters *hc = (const BfsCounters *)c->h_bfs_ctr;
-    const int n = std::min(hc->levels, BFS_TRACE_LEVELS);
     *nlevels = hc->levels;
+    const int n = std::min(hc->levels, BFS_TRACE_LEVELS);
     for (int l = 0; l < n && l < cap; ++l) {
-        // level l expands queue [tail[l-1], tail[l]) -- the vertices at distance l
-        const long long b = l == 0 ? 0 : hc->trace.tail[l - 1], e = hc->trace.tail[l];
         if (level_ns) level_ns[l] = (int64_t)(hc->trace.ns[l + 1] - hc->trace.ns[l]);
-        if (frontier) frontier[l] = e - b;
-        if (entries) entries[l] = (int64_t)(hc->trace.reads[l + 1] - hc->trace.reads[l]);
+        if (frontier) frontier[l] = hc->trace.frontier[l];
+        if (entries) entries[l] = (int64_t)hc->trace.entries[l];
     }
     return FC_OK;
 }

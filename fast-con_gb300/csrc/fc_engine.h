@@ -89,17 +89,16 @@ struct DevCtx {
     // staging of host-array batches (queries in, answers out)
     int32_t *b_stage = nullptr;
     size_t b_stage_cap = 0;
-    // plain BFS engine (fc_bfs.cu): visited bitmap, levels and queue in the
-    // search's numbering, levels in the caller's numbering, counters, row jobs
+    // plain BFS engine (fc_bfs.cu): visited bitmap, levels in the search's
+    // numbering and in the caller's, frontier queues, counters
     unsigned *bfs_bm = nullptr;
     int32_t *bfs_lev = nullptr;
-    int32_t *bfs_q = nullptr;
     int32_t *bfs_out = nullptr;
+    int2 *bfs_q = nullptr;           // frontier queues (row ranges)
     size_t bfs_nv = 0;
+    long long bfs_pcap = 0;
     void *bfs_ctr = nullptr;
     void *h_bfs_ctr = nullptr;
-    int2 *bfs_jobs = nullptr;
-    int bfs_jcap = 0;
 };
 
 // Device staging for a host-array batch of n queries: 5n ints, kept between
@@ -117,7 +116,7 @@ struct BfsLayout;
 int bfs_layout_build(const GraphPairH &gp, BfsLayout **out, cudaStream_t st, int only_if_skewed);
 void bfs_layout_free(BfsLayout *L);
 int engine_bfs_plain(DevCtx *c, const GraphPairH &gp, const BfsLayout *L, int32_t s,
-                     int32_t *h_levels, fc_stats *st, cudaStream_t stream);
+                     int32_t *h_levels, const fc_opts &o, fc_stats *st, cudaStream_t stream);
 int engine_bfs_trace(DevCtx *c, int32_t *nlevels, int64_t *level_ns, int64_t *frontier,
                      int64_t *entries, int32_t cap);
 

@@ -158,16 +158,21 @@ __device__ __forceinline__ int grid_barrier_snap(int *bar, int *err, int nblocks
             __threadfence();
             st_release_gpu(bar + 1, gen + 1);
         } else {
+            // pollers back off (64 ns doubling to 512 ns): hundreds of CTAs
+            // polling one word at a fixed short interval load its L2 slice
+            // enough to slow the atomics of the CTAs still working
             unsigned long long t0 = global_timer_ns();
             long long spins = 0;
+            unsigned pause = 64;
             while (ld_acquire_gpu(bar + 1) == gen) {
                 if (++spins > BARRIER_MAX_SPINS ||
-                    ((spins & 255) == 0 && global_timer_ns() - t0 > timeout_ns)) {
+                    ((spins & 63) == 0 && global_timer_ns() - t0 > timeout_ns)) {
                     atomicCAS(err, 0, FC_ERR_TIMEOUT);
                     ok = 0;
                     break;
                 }
-                __nanosleep(64);
+                __nanosleep(pause);
+                if (pause < 512) pause <<= 1;
             }
         }
         if (ok && ld_acquire_gpu(err) != 0) ok = 0;

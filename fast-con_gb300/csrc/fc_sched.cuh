@@ -26,7 +26,6 @@ struct TeamCounters {
     int err;
     unsigned long long deg[2];
     unsigned long long inspected;  // bottom-up adjacency reads
-    int bar[2];
     int invalid;
     int pad;
     unsigned long long hist[2];     // claimed vertices per side of degree < 8 (low 32 bits)
@@ -34,6 +33,9 @@ struct TeamCounters {
     int njobs[2];                   // row-job slots taken, by step parity
     int nok[2];                     // row jobs written (a prefix of the slots)
     TeamSnap snap[2];               // by barrier generation parity
+    // grid barrier words in a line of their own: waiting CTAs poll them
+    // while the working ones update the counters above
+    alignas(128) int bar[2];
 };
 
 struct SnapTeam {

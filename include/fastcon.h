@@ -62,7 +62,8 @@ typedef struct fc_opts {
     int32_t sched;        /* FC_SCHED_*                                     */
     int32_t engine;       /* FC_ENGINE_*                                    */
     int32_t block;        /* threads per CTA: 128, 256 or 512 (0 = tuned)   */
-    int32_t ctas_per_sm;  /* resident CTAs per SM for batched (0 = 3)       */
+    int32_t ctas_per_sm;  /* resident CTAs per SM: batched (0 = 3); plain BFS
+                             engine 2, 3 or 4 (0 = 4)                       */
     int32_t use_graph;    /* batched: capture the launch in a CUDA graph    */
     int32_t max_slots;    /* batched: cap on concurrent queries (0 = all)   */
     void   *stream;       /* cudaStream_t, NULL = the library's own stream  */
