@@ -362,6 +362,46 @@ int fc_graph_generate_rmat(int32_t scale, int64_t nedges, double a, double b, do
     return rc;
 }
 
+int fc_graph_generate_graph500(int32_t scale, int64_t nedges, uint64_t seed1, uint64_t seed2,
+                               const double *initiator, fc_graph **g)
+{
+    if (validate_ptr(g, "g")) return FC_ERR_INVALID;
+    *g = nullptr;
+    static const double graph500_default[4] = {.57, .19, .19, .05};
+    CtxLock L;
+    if (!L.c) return L.rc;
+    cudaStream_t st = L.c->stream;
+    int32_t *ds = nullptr, *dd = nullptr;
+    int rc = fc::gen_graph500_device(scale, nedges, seed1, seed2,
+                                     initiator ? initiator : graph500_default, &ds, &dd, st);
+    if (rc == FC_OK) rc = from_device_edges(ds, dd, nedges, 1 << scale, 0, g, st);
+    cudaStreamSynchronize(st);
+    cudaFree(ds);
+    cudaFree(dd);
+    return rc;
+}
+
+int fc_graph_generate_graph500_edges(int32_t scale, int64_t nedges, uint64_t seed1,
+                                     uint64_t seed2, const double *initiator, int32_t *src,
+                                     int32_t *dst)
+{
+    if (validate_ptr(src, "src") || validate_ptr(dst, "dst")) return FC_ERR_INVALID;
+    static const double graph500_default[4] = {.57, .19, .19, .05};
+    CtxLock L;
+    if (!L.c) return L.rc;
+    cudaStream_t st = L.c->stream;
+    int32_t *ds = nullptr, *dd = nullptr;
+    int rc = fc::gen_graph500_device(scale, nedges, seed1, seed2,
+                                     initiator ? initiator : graph500_default, &ds, &dd, st);
+    if (rc == FC_OK) {
+        FC_CUDA_TRY(cudaMemcpy(src, ds, sizeof(int32_t) * (size_t)nedges, cudaMemcpyDeviceToHost));
+        FC_CUDA_TRY(cudaMemcpy(dst, dd, sizeof(int32_t) * (size_t)nedges, cudaMemcpyDeviceToHost));
+    }
+    cudaFree(ds);
+    cudaFree(dd);
+    return rc;
+}
+
 int fc_graph_generate_grid(int32_t w, int32_t h, double p_del, uint64_t del_seed, int64_t shortcuts,
                            uint64_t sc_seed, fc_graph **g)
 {

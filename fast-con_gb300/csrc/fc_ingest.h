@@ -20,6 +20,11 @@ int gen_rmat_device(int scale, long long nedges, double a, double b, double c,
 // Exclusive scan of n int32 values into out[0..n), out[n] = total (int64).
 int scan_i32(const int32_t *in, long long n, long long *out, cudaStream_t st);
 
+// M edges of the Graph500 generator (fc_g500.cu) into new device arrays.
+int gen_graph500_device(int scale, long long m, unsigned long long seed1, unsigned long long seed2,
+                        const double initiator[4], int32_t **d_src, int32_t **d_dst,
+                        cudaStream_t st);
+
 long long grid_edge_slots(int w, int h, long long shortcuts);
 
 int gen_grid_device(int w, int h, double p_del, unsigned long long del_seed, long long shortcuts,

@@ -37,7 +37,7 @@ EXPORTS = [
     "fc_opts_init", "fc_graph_load_edgelist", "fc_graph_from_csr", "fc_graph_from_edges",
     "fc_graph_from_device_edges", "fc_graph_generate_rmat", "fc_graph_generate_grid",
     "fc_graph_info", "fc_graph_get_csr", "fc_graph_free", "fc_bfs_levels", "fc_bfs_levels_ex",
-    "fc_bfs_trace",
+    "fc_bfs_trace", "fc_graph_generate_graph500", "fc_graph_generate_graph500_edges",
     "fc_stcon", "fc_stcon_ex", "fc_stcon_depth", "fc_stcon_batch", "fc_stcon_batch_device",
     "fc_stcon_batch_noalloc", "fc_sched_set_weights", "fc_sched_get_weights",
     "fc_mlp_loss_grad", "fc_mlp_train", "fc_stcon_batch_scripted", "fc_selftest_wait",
@@ -103,6 +103,11 @@ def lib():
                                                       ctypes.c_double, ctypes.c_uint64, _I64, _VP]),
             "fc_graph_generate_grid": (ctypes.c_int, [_I32, _I32, ctypes.c_double, ctypes.c_uint64,
                                                       _I64, ctypes.c_uint64, _VP]),
+            "fc_graph_generate_graph500": (ctypes.c_int, [_I32, _I64, ctypes.c_uint64,
+                                                          ctypes.c_uint64, _VP, _VP]),
+            "fc_graph_generate_graph500_edges": (ctypes.c_int, [_I32, _I64, ctypes.c_uint64,
+                                                                ctypes.c_uint64, _VP, _VP, _VP]),
+            "fc_bfs_trace": (ctypes.c_int, [_VP, _VP, _VP, _VP, _I32]),
             "fc_graph_info": (ctypes.c_int, [_VP, _VP, _VP, _VP]),
             "fc_graph_get_csr": (ctypes.c_int, [_VP, _VP, _VP]),
             "fc_graph_free": (None, [_VP]),
@@ -225,6 +230,14 @@ class Graph:
              perm_seed: int = -1) -> "Graph":
         return cls._make(lib().fc_graph_generate_rmat, int(scale), int(nedges), float(a), float(b),
                          float(c), int(seed), int(perm_seed), what="fc_graph_generate_rmat")
+
+    @classmethod
+    def graph500(cls, scale: int, nedges: int, seed1: int, seed2: int,
+                 initiator=(0.57, 0.19, 0.19, 0.05)) -> "Graph":
+        """The reference driver's Graph500 graph (make_graph), made on the device."""
+        ini = np.ascontiguousarray(initiator, dtype=np.float64)
+        return cls._make(lib().fc_graph_generate_graph500, int(scale), int(nedges), int(seed1),
+                         int(seed2), _P(ini), what="fc_graph_generate_graph500")
 
     @classmethod
     def grid(cls, w: int, h: int, p_del=0.05, del_seed: int = 5, shortcuts: int = 0,
@@ -429,6 +442,18 @@ def bfs_trace(cap: int = 256):
     _check(lib().fc_bfs_trace(ctypes.byref(n), _P(ns), _P(fr), _P(en), int(cap)), "fc_bfs_trace")
     k = min(n.value, cap)
     return {"levels": n.value, "level_ns": ns[:k], "frontier": fr[:k], "entries": en[:k]}
+
+
+def graph500_edges(scale: int, nedges: int, seed1: int, seed2: int,
+                   initiator=(0.57, 0.19, 0.19, 0.05)):
+    """Raw edge list of the Graph500 generator (device), int32 (src, dst)."""
+    ini = np.ascontiguousarray(initiator, dtype=np.float64)
+    src = np.zeros(nedges, np.int32)
+    dst = np.zeros(nedges, np.int32)
+    _check(lib().fc_graph_generate_graph500_edges(int(scale), int(nedges), int(seed1), int(seed2),
+                                                  _P(ini), _P(src), _P(dst)),
+           "fc_graph_generate_graph500_edges")
+    return src, dst
 
 
 def device_info():

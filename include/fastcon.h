@@ -173,6 +173,24 @@ int fc_graph_from_device_edges(const int32_t *d_src, const int32_t *d_dst, int64
  * bijection when perm_seed >= 0. */
 int fc_graph_generate_rmat(int32_t scale, int64_t nedges, double a, double b, double c,
                            uint64_t seed, int64_t perm_seed, fc_graph **g);
+/* The Graph500 Kronecker graph the reference driver generates, made on the
+ * device: the edges of make_graph(scale, nedges, seed1, seed2, initiator)
+ * (bernaschi/ST_CONN_ONE_ATOMIC/current-st/generator/make_graph.c:35-104,
+ * called at S/main.c:370), bit for bit, followed by run_make_struct
+ * (symmetrise, drop self-loops, deduplicate).  initiator (nullable) = the
+ * four quadrant probabilities a, b, c, d (default .57, .19, .19, .05).
+ * 1 <= scale <= 29. */
+int fc_graph_generate_graph500(int32_t scale, int64_t nedges, uint64_t seed1, uint64_t seed2,
+                               const double *initiator, fc_graph **g);
+/* The same generator's raw edge list (host arrays of nedges entries): both
+ * ends in the generator's vertex labels, the smaller first, self-loops and
+ * repeated edges kept as make_graph keeps them; in the generator's own order
+ * before its final shuffle of the list (scramble_edges_shared), which this
+ * does not apply. */
+int fc_graph_generate_graph500_edges(int32_t scale, int64_t nedges, uint64_t seed1,
+                                     uint64_t seed2, const double *initiator, int32_t *src,
+                                     int32_t *dst);
+
 /* w x h 4-neighbour grid, each edge dropped with probability p_del, plus
  * `shortcuts` uniformly random extra edges. */
 int fc_graph_generate_grid(int32_t w, int32_t h, double p_del, uint64_t del_seed,

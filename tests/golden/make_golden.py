@@ -20,6 +20,10 @@ What it writes (all small, all committed):
   and bernaschi's ``load_graph`` (``oracle/_ref/libref_loadgraph.so``):
   vertex count, direction, the COO list in the reader's order and the CSR,
   as SHA-256 digests plus the full arrays of the small files.
+* ``ref_graph500.json`` -- the reference's Graph500 generator (make_graph,
+  ``oracle/_ref/graph500_gen``) at a few sizes and seeds: its raw edge list
+  (both ends, smaller first, self-loops and repeats kept) sorted, and the
+  canonical CSR built from it, as SHA-256 digests and counts.
 * ``ref_bfs_*.json`` -- outputs of the reference's own CPU BFS
   (``Graph::bfs``, BFS-4K/src/host/graph.cpp:83-97, compiled into
   ``oracle/_ref/libref_bfs.so``) on the ER workload (65,536 vertices,
@@ -125,11 +129,37 @@ def reader_fixtures():
     json.dump(out, open(os.path.join(HERE, "ref_readers.json"), "w"), indent=1)
 
 
+GRAPH500_CASES = [(8, 16, 1, 2), (10, 16, 1, 2), (12, 16, 77, 991), (14, 8, 5, 6),
+                  (16, 16, 670021781, 1422323141)]
+
+
+def graph500_fixtures():
+    """ref_graph500.json from the reference generator."""
+    out = []
+    with tempfile.TemporaryDirectory() as td:
+        for scale, ef, s1, s2 in GRAPH500_CASES:
+            path = os.path.join(td, "e.bin")
+            subprocess.run([oracle.REF_GEN_PATH, str(scale), str(ef), str(s1), str(s2), path],
+                           check=True, stdout=subprocess.DEVNULL)
+            e = np.fromfile(path, dtype=np.int64).reshape(-1, 2)
+            lo = np.minimum(e[:, 0], e[:, 1]).astype(np.int32)
+            hi = np.maximum(e[:, 0], e[:, 1]).astype(np.int32)
+            o = np.lexsort((hi, lo))
+            pairs = np.stack([lo[o], hi[o]], 1)
+            nv = 1 << scale
+            rp, col = oracle.build_csr(nv, lo, hi)
+            out.append({"scale": scale, "edgefactor": ef, "seed1": s1, "seed2": s2,
+                        "nedges": int(len(e)), "self_loops": int((lo == hi).sum()),
+                        "sorted_edges_sha256": sha_levels(pairs.reshape(-1)),
+                        "directed_entries": int(len(col)), "csr_sha256": sha_csr(rp, col)})
+    json.dump(out, open(os.path.join(HERE, "ref_graph500.json"), "w"), indent=1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("FASTCON_REFERENCE", ""),
                     help="root of the reference tree")
-    ap.add_argument("--only", default=None, choices=["readers"],
+    ap.add_argument("--only", default=None, choices=["readers", "graph500"],
                     help="write only this fixture")
     args = ap.parse_args()
     if not args.ref or not os.path.isdir(args.ref):
@@ -137,6 +167,9 @@ def main():
     oracle.build(args.ref)
     if args.only == "readers":
         reader_fixtures()
+        return
+    if args.only == "graph500":
+        graph500_fixtures()
         return
 
     # 1. known-answer rows
@@ -228,6 +261,8 @@ def main():
 
     # 5. the edge-list readers
     reader_fixtures()
+    # 6. the Graph500 generator
+    graph500_fixtures()
     print("fixtures written to", HERE)
 
 
