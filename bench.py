@@ -474,7 +474,7 @@ def run_fastcon(args, cfg):
     # repeated batches of one shape: the library replays one captured CUDA
     # graph per batch (use_graph), as a serving loop would
     opt = fc.make_opts(sched=sched, engine=fc.ENGINE_BATCHED, stream=stream.cuda_stream,
-                       use_graph=1)
+                       use_graph=1, max_slots=args.max_slots)
     d_s = torch.from_numpy(s).cuda()
     d_t = torch.from_numpy(t).cuda()
     d_g = torch.from_numpy(gi).cuda() if gi is not None else None
@@ -722,6 +722,9 @@ def main():
     ap.add_argument("--impl", default="fastcon", choices=["fastcon", "reference"])
     ap.add_argument("--config", default="rmat24", choices=sorted(CONFIGS))
     ap.add_argument("--sched", default="learned", choices=["heuristic", "plain", "learned"])
+    ap.add_argument("--max-slots", type=int, default=0,
+                    help="cap on the batch's concurrent query slots (0 = all resident CTAs); "
+                         "small profiler captures only")
     ap.add_argument("--bfs", default=None, choices=["plain", "heuristic"],
                     help="time one full BFS of the workload's graph instead of the batch")
     ap.add_argument("--engine", default="auto", choices=["auto", "hostloop", "persistent"],

@@ -715,6 +715,31 @@ int fc_stcon_multiseed(fc_graph *g, int32_t s, int32_t t, int32_t nseeds, uint64
                                       L.c->stream);
 }
 
+int fc_selftest_primitives(int32_t which, const int32_t *in, int32_t n, int32_t *out,
+                           int32_t *aux)
+{
+    if (which < 0 || which > 3 || n < 0 || (n > 0 && (!in || !out))) {
+        set_error("fc_selftest_primitives: which %d, n %d", which, n);
+        return FC_ERR_INVALID;
+    }
+    if (which == 3)
+        for (int32_t i = 0; i < n; ++i)
+            if (in[i] < -1) {
+                set_error("fc_selftest_primitives: value %d below -1", in[i]);
+                return FC_ERR_INVALID;
+            }
+    if (which == 2)
+        for (int32_t i = 0; i < n; ++i)
+            if (in[i] < 0) {
+                set_error("fc_selftest_primitives: negative row length");
+                return FC_ERR_INVALID;
+            }
+    if (n == 0) return FC_OK;
+    CtxLock L;
+    if (!L.c) return L.rc;
+    return fc::engine_selftest_primitives(L.c, which, in, n, out, aux, L.c->stream);
+}
+
 int fc_selftest_wait(int32_t timeout_ms, double *elapsed_ms)
 {
     if (timeout_ms < 1 || timeout_ms > 2000) {

@@ -168,6 +168,10 @@ int ensure_workspace(DevCtx *c, size_t nv);
 // expires; returns FC_ERR_TIMEOUT when it did.
 int engine_selftest_wait(DevCtx *c, int timeout_ms, double *elapsed_ms, cudaStream_t stream);
 
+// The scan / compaction / search primitives on caller data (fc_selftest.cu).
+int engine_selftest_primitives(DevCtx *c, int which, const int32_t *h_in, int n, int32_t *h_out,
+                               int32_t *h_aux, cudaStream_t st);
+
 void set_error(const char *fmt, ...);
 
 }  // namespace fc

@@ -38,6 +38,7 @@ EXPORTS = [
     "fc_graph_from_device_edges", "fc_graph_generate_rmat", "fc_graph_generate_grid",
     "fc_graph_info", "fc_graph_get_csr", "fc_graph_free", "fc_bfs_levels", "fc_bfs_levels_ex",
     "fc_bfs_trace", "fc_graph_generate_graph500", "fc_graph_generate_graph500_edges",
+    "fc_selftest_primitives",
     "fc_stcon", "fc_stcon_ex", "fc_stcon_depth", "fc_stcon_batch", "fc_stcon_batch_device",
     "fc_stcon_batch_noalloc", "fc_sched_set_weights", "fc_sched_get_weights",
     "fc_mlp_loss_grad", "fc_mlp_train", "fc_stcon_batch_scripted", "fc_selftest_wait",
@@ -108,6 +109,7 @@ def lib():
             "fc_graph_generate_graph500_edges": (ctypes.c_int, [_I32, _I64, ctypes.c_uint64,
                                                                 ctypes.c_uint64, _VP, _VP, _VP]),
             "fc_bfs_trace": (ctypes.c_int, [_VP, _VP, _VP, _VP, _I32]),
+            "fc_selftest_primitives": (ctypes.c_int, [_I32, _VP, _I32, _VP, _VP]),
             "fc_graph_info": (ctypes.c_int, [_VP, _VP, _VP, _VP]),
             "fc_graph_get_csr": (ctypes.c_int, [_VP, _VP, _VP]),
             "fc_graph_free": (None, [_VP]),
@@ -454,6 +456,23 @@ def graph500_edges(scale: int, nedges: int, seed1: int, seed2: int,
                                                   _P(ini), _P(src), _P(dst)),
            "fc_graph_generate_graph500_edges")
     return src, dst
+
+
+def selftest_primitives(which: int, data):
+    """Run one of the library's primitives on `data` (see fc_selftest_primitives):
+    returns (out, aux)."""
+    a = _i32(data)
+    n = len(a)
+    if which == 2:
+        out = np.zeros(max(1, int(a.sum())), np.int32)
+    else:
+        out = np.zeros(max(1, n), np.int32)
+    aux = np.zeros(max(1, (n + 255) // 256), np.int32)
+    _check(lib().fc_selftest_primitives(int(which), _P(a) if n else None, n, _P(out), _P(aux)),
+           "fc_selftest_primitives")
+    if which == 2:
+        return out[: int(a.sum())], aux
+    return out[:n], aux
 
 
 def device_info():

@@ -380,6 +380,22 @@ int fc_stcon_multiseed(fc_graph *g, int32_t s, int32_t t, int32_t nseeds, uint64
  * another code on failure; *elapsed_ms (nullable) gets the kernel's time. */
 int fc_selftest_wait(int32_t timeout_ms, double *elapsed_ms);
 
+/* Self-test of the scan, compaction and search primitives the expansion steps
+ * use, on caller data (host arrays; no counterpart in the reference, which
+ * takes these from Thrust and CUB: S/mythrustlib.cu:25-34,175-185, checked by
+ * check_queue_off, S/test/gputestfunc.cu:225-258).
+ *   which 0: out[i] = inclusive warp scan of in within each group of 32;
+ *   which 1: out[i] = inclusive block scan within each group of 256,
+ *            aux[g] = group g's total;
+ *   which 2: in = row lengths, 256 rows to a tile; for every entry of each
+ *            tile's rows laid end to end, out = the row (0..255) the
+ *            load-balanced search finds (out holds sum(in) entries);
+ *   which 3: in = values >= 0 to append (-1 = none), one CTA offering eight
+ *            per thread and round; out = the log the per-warp claim buffers
+ *            write, aux[0] = its length (each offered value exactly once). */
+int fc_selftest_primitives(int32_t which, const int32_t *in, int32_t n, int32_t *out,
+                           int32_t *aux);
+
 /* ---- misc ---------------------------------------------------------------- */
 const char *fc_strerror(int code);
 const char *fc_last_error_message(void);  /* thread-local detail of the last error */
