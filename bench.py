@@ -321,9 +321,20 @@ def plain_bfs_block(fc, G, peak, nsrc=4, reps=5):
         per.append({"source": src, "ms": m, "levels": int(lev.max()) + 1,
                     "entries": int(st["edges_inspected"]), "reached": int((lev >= 0).sum())})
     achieved = tot_bytes / 1e9 / (tot_ms / 1e3)
+    # DRAM bytes of the search: a small-case ncu capture of the same kernel,
+    # scaled by the algorithmic bytes (both grow per entry and per vertex)
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic_per_unit.json")
+    if os.path.exists(tp):
+        ratio = json.load(open(tp)).get("k_bfs_plain", {}).get("dram_bytes_per_alg_byte")
+        if ratio:
+            traffic = float(ratio) * tot_bytes / len(srcs)
     return {"form": "full BFS, plain schedule (level-synchronous, top-down), library default engine",
+            "kernel": "k_bfs_plain",
             "ms": tot_ms / len(srcs), "alg_bytes": tot_bytes / len(srcs),
             "achieved_gbs": achieved, "peak": peak, "frac": achieved / peak,
+            "traffic": traffic,
+            "traffic_source": "profiles/traffic_per_unit.json (scaled small-case capture)",
             "gteps_entries": tot_entries / (tot_ms * 1e6), "sources": per,
             "bytes_rule": "8 per adjacency entry read + 20 per reached vertex",
             "_source": srcs[0], "_levels": lev0}
