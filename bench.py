@@ -56,8 +56,10 @@ CONFIGS = {
     "grid4096": dict(kind="grid", w=4096, h=4096, p_del=0.05, del_seed=5, sc_seed=6, nq=256,
                      qseed=7, min_manhattan=2000),
     "batched512": dict(kind="multi", ngraphs=512, first_seed=100, per_graph=8),
-    # smaller R-MAT (same parameters) used for profiler captures
+    # smaller R-MATs (same parameters) used for profiler captures
     "rmat22": dict(kind="rmat", scale=22, edge_samples=8 << 22, seed=3, perm_seed=3, nq=1024,
+                   qseed=4),
+    "rmat21": dict(kind="rmat", scale=21, edge_samples=8 << 21, seed=3, perm_seed=3, nq=1024,
                    qseed=4),
 }
 

@@ -360,13 +360,46 @@ def silence_variant_head(w):
     return w
 
 
+def heldout_evaluation(eval_queries=4096, reps=5):
+    """The learned schedule against the heuristic and the plain one on the
+    held-out sets: R-MAT scale 24 (seed 9) and the 4096 x 4096 grid, 4,096
+    pairs each; answers compared with the plain schedule's (the tests compare
+    all three with the CPU oracle)."""
+    ev = {}
+    G = Graph.rmat(24, 8 << 24, seed=9, perm_seed=9)
+    rp, _ = G.csr_row_ptr()
+    s, t = graphs.pairs_with_degree(np.diff(rp), eval_queries, seed=9)
+    ref = stcon_batch(G, s, t, opts=make_opts(sched=SCHED_PLAIN, engine=ENGINE_BATCHED))[1]
+    ev["rmat24_seed9"] = evaluate(G, s, t, ref, reps=reps)
+    G.free()
+    n = 4096 * 4096
+    G = Graph.grid(4096, 4096, p_del=0.05, del_seed=5, shortcuts=graphs.grid_shortcut_count(n),
+                   sc_seed=6)
+    s, t = graphs.grid_pairs(4096, 4096, eval_queries, 17, 2000)
+    ref = stcon_batch(G, s, t, opts=make_opts(sched=SCHED_PLAIN, engine=ENGINE_BATCHED))[1]
+    ev["grid4096"] = evaluate(G, s, t, ref, reps=reps)
+    G.free()
+    return ev
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--queries", type=int, default=20000)
     ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--out", default=WEIGHTS_PATH)
     ap.add_argument("--eval-queries", type=int, default=4096)
+    ap.add_argument("--evaluate-only", action="store_true",
+                    help="re-measure the committed weights on the held-out sets with the current "
+                         "kernels and rewrite only the evaluation record")
     args = ap.parse_args()
+    if args.evaluate_only:
+        meta = json.load(open(args.out))
+        load_default_weights(args.out)
+        meta["evaluation"] = heldout_evaluation(args.eval_queries)
+        with open(args.out, "w") as f:
+            json.dump(meta, f, indent=1)
+        print(json.dumps(meta["evaluation"], indent=1))
+        return
     t0 = time.time()
     X, Y, SW, C, A, P = build_dataset(args.queries)
     t1 = time.time()
@@ -405,20 +438,7 @@ def main():
               "learned": policy_regret(Xv[:nval], Cv, Av, Pv, w), "round1": r1}
     t2 = time.time()
     set_weights(w, box)
-    ev = {}
-    G = Graph.rmat(24, 8 << 24, seed=9, perm_seed=9)
-    rp, _ = G.csr_row_ptr()
-    s, t = graphs.pairs_with_degree(np.diff(rp), args.eval_queries, seed=9)
-    ref = stcon_batch(G, s, t, opts=make_opts(sched=SCHED_PLAIN, engine=ENGINE_BATCHED))[1]
-    ev["rmat24_seed9"] = evaluate(G, s, t, ref)
-    G.free()
-    n = 4096 * 4096
-    G = Graph.grid(4096, 4096, p_del=0.05, del_seed=5, shortcuts=graphs.grid_shortcut_count(n),
-                   sc_seed=6)
-    s, t = graphs.grid_pairs(4096, 4096, args.eval_queries, 17, 2000)
-    ref = stcon_batch(G, s, t, opts=make_opts(sched=SCHED_PLAIN, engine=ENGINE_BATCHED))[1]
-    ev["grid4096"] = evaluate(G, s, t, ref)
-    G.free()
+    ev = heldout_evaluation(args.eval_queries)
     meta = {
         "weights": [float(x) for x in w],
         "box": {"lo": [float(x) for x in box[0]], "hi": [float(x) for x in box[1]]},
