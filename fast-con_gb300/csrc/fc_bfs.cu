@@ -159,6 +159,16 @@ __global__ void k_layout_cols(const int32_t *row_ptr, const int32_t *col, const 
     }
 }
 
+void bfs_layout_graph(const BfsLayout *L, DGraphH *out)
+{
+    out->row_ptr = L->row_ptr;
+    out->col = L->col;
+    out->nv = L->nv;
+    out->pad_ = 0;
+    out->ne = L->ne;
+    out->remap = L->new_id;
+}
+
 void bfs_layout_free(BfsLayout *L)
 {
     if (!L) return;

@@ -106,6 +106,31 @@ struct PersistArgs {
     int jcap;
 };
 
+// One step of k_persistent and its row jobs.
+template <int T>
+__device__ __forceinline__ void persist_step(const PersistArgs &a, const GraphPair &gp, const QLocal &ql,
+                                          int x, const int32_t *front, int F, int par,
+                                          SmemTopDown<T> &sm)
+{
+    TeamCounters *tc = a.tc;
+    const int nv = gp.fwd.nv;
+    run_step<T>(a.mode, gp, x, ql.dir, ql.radius[x], ql.radius[1 - x], front, F, blockIdx.x,
+                gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x], &tc->deg[x], &tc->found,
+                &tc->inspected, sm, ql.variant, a.mlp ? &tc->hist[x] : nullptr,
+                TeamSink{a.jobs, a.jcap, &tc->njobs[par], &tc->nok[par]},
+                team_tile_v<T>(F, (long long)(ql.dt[x] - ql.dh[x])));
+}
+
+template <int T>
+__device__ __forceinline__ void persist_jobs(const PersistArgs &a, const GraphPair &gp, const QLocal &ql,
+                                          int x, int nj, SmemTopDown<T> &sm)
+{
+    TeamCounters *tc = a.tc;
+    run_team_jobs<T>(a.mode, gp, x, ql.radius[x], a.jobs, nj, blockIdx.x, gridDim.x, a.status,
+                     a.levels, a.log, gp.fwd.nv, &tc->tail[x], &tc->deg[x], &tc->found, sm,
+                     a.mlp ? &tc->hist[x] : nullptr, &tc->inspected);
+}
+
 template <int T>
 __global__ void __launch_bounds__(T, 768 / T) k_persistent(PersistArgs a)
 {
@@ -117,8 +142,8 @@ __global__ void __launch_bounds__(T, 768 / T) k_persistent(PersistArgs a)
         const int q = a.list ? a.list[li] : li;
         const GraphPair gp = a.graphs[a.graph_idx ? a.graph_idx[q] : 0];
         const int nv = gp.fwd.nv;
-        const int s = a.qs[q];
-        const int t = a.mode == MODE_STCON ? a.qt[q] : s;
+        int s = a.qs[q];
+        int t = a.mode == MODE_STCON ? a.qt[q] : s;
         const bool bad = s < 0 || s >= nv || t < 0 || t >= nv;
         if (bad) {  // uniform across the grid: no barrier needed to skip
             if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -127,6 +152,10 @@ __global__ void __launch_bounds__(T, 768 / T) k_persistent(PersistArgs a)
                 atomicExch(&tc->invalid, 1);
             }
             continue;
+        }
+        if (gp.fwd.remap) {  // a renumbered copy of the graph: the caller's ids map into it
+            s = __ldg(gp.fwd.remap + s);
+            t = __ldg(gp.fwd.remap + t);
         }
         if (blockIdx.x == 0 && threadIdx.x == 0)
             init_roots(a.mode, gp, s, t, a.status, a.levels, a.log, nv, tc);
@@ -165,12 +194,7 @@ __global__ void __launch_bounds__(T, 768 / T) k_persistent(PersistArgs a)
                 tc->njobs[par ^ 1] = 0;
                 tc->nok[par ^ 1] = 0;
             }
-            run_step<T>(a.mode, gp, x, ql.dir, ql.radius[x], ql.radius[1 - x], front, F,
-                        blockIdx.x, gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x],
-                        &tc->deg[x], &tc->found, &tc->inspected, sm, ql.variant,
-                        a.mlp ? &tc->hist[x] : nullptr,
-                        TeamSink{a.jobs, a.jcap, &tc->njobs[par], &tc->nok[par]},
-                        team_tile_v<T>(F, (long long)(ql.dt[x] - ql.dh[x])));
+            persist_step<T>(a, gp, ql, x, front, F, par, sm);
             g = grid_barrier_snap(tc->bar, &tc->err, gridDim.x, SnapTeam{tc});
             if (g < 0) return;
             if (ql.dir == DIR_TD) {
@@ -178,9 +202,7 @@ __global__ void __launch_bounds__(T, 768 / T) k_persistent(PersistArgs a)
                 if (threadIdx.x == 0) s_nj = min(ld_cg(&tc->snap[g & 1].nok[par]), a.jcap);
                 __syncthreads();
                 if (s_nj > 0) {  // same value in every CTA: uniform barrier
-                    run_team_jobs<T>(a.mode, gp, x, ql.radius[x], a.jobs, s_nj, blockIdx.x,
-                                     gridDim.x, a.status, a.levels, a.log, nv, &tc->tail[x],
-                                     &tc->deg[x], &tc->found, sm, a.mlp ? &tc->hist[x] : nullptr, &tc->inspected);
+                    persist_jobs<T>(a, gp, ql, x, s_nj, sm);
                     g = grid_barrier_snap(tc->bar, &tc->err, gridDim.x, SnapTeam{tc});
                     if (g < 0) return;
                 }

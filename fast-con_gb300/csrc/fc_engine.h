@@ -16,6 +16,7 @@ struct DGraphH {  // host copy of a device CSR
     int32_t nv;
     int32_t pad_;
     int64_t ne;
+    const int32_t *remap;  // nullable: caller's vertex id -> id in this CSR (a renumbered copy)
 };
 
 // forward CSR (expands the s side) and reverse CSR (expands the t side);
@@ -115,6 +116,9 @@ int engine_bfs(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_levels,
 struct BfsLayout;
 int bfs_layout_build(const GraphPairH &gp, BfsLayout **out, cudaStream_t st, int only_if_skewed);
 void bfs_layout_free(BfsLayout *L);
+// The renumbered CSR of a layout as a graph a batch can run on (remap = the
+// caller's id -> renumbered id map).
+void bfs_layout_graph(const BfsLayout *L, DGraphH *out);
 int engine_bfs_plain(DevCtx *c, const GraphPairH &gp, const BfsLayout *L, int32_t s,
                      int32_t *h_levels, const fc_opts &o, fc_stats *st, cudaStream_t stream);
 int engine_bfs_trace(DevCtx *c, int32_t *nlevels, int64_t *level_ns, int64_t *frontier,

@@ -43,6 +43,7 @@ struct DGraph {
     int32_t nv;
     int32_t pad_;
     int64_t ne;
+    const int32_t *remap;  // nullable: caller's vertex id -> id in this CSR
 };
 
 // ---------------------------------------------------------------------------

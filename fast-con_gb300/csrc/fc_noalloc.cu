@@ -225,6 +225,7 @@ extern "C" int fc_stcon_batch_noalloc(const int32_t *d_row_ptr, const int32_t *d
     gp.fwd.col = d_col;
     gp.fwd.nv = nv;
     gp.fwd.pad_ = 0;
+    gp.fwd.remap = nullptr;
     gp.fwd.ne = ne;
     gp.rev = gp.fwd;
     if (d_rrow_ptr) {

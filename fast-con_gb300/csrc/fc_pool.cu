@@ -119,7 +119,8 @@ template <int T>
 struct SmemPool {
     SmemTopDown<T> td;
     QLocal ql;
-    PoolDesc d;  // description of the step whose tile this CTA is running
+    PoolDesc d;    // description of the step whose tile this CTA is running
+    PoolDesc own;  // the owner's description of its query's steps (thread 0 writes it)
     int q, li, publish, flag, cand, claimed, cursor;
     unsigned seq, my_seq;
     int err;
@@ -431,6 +432,18 @@ __device__ void pool_publish_and_run(const PoolArgs &a, PoolSlot *my, const Pool
     __syncthreads();
 }
 
+// A step the owner runs alone.
+template <int T>
+__device__ __forceinline__ void pool_private_step(int mode, const GraphPair &gp, int x, int level,
+                                               int other_radius, const int32_t *front, int F,
+                                               uint8_t *status, int32_t *levels, int32_t *log,
+                                               int cap, SmemPool<T> &sm, int variant, bool track)
+{
+    run_step<T>(mode, gp, x, DIR_TD, level, other_radius, front, F, 0, 1, status, levels, log, cap,
+                &sm.stc.tail[x], &sm.stc.deg[x], &sm.stc.found, &sm.stc.inspected, sm.td, variant,
+                track ? &sm.stc.hist[x] : nullptr);
+}
+
 // Run query q with my slot as owner.
 template <int T>
 __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *status, int32_t *log,
@@ -440,8 +453,8 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
     const int gidx = a.graph_idx ? a.graph_idx[q] : 0;
     const GraphPair gp = a.graphs[gidx];
     const int nv = gp.fwd.nv;
-    const int s = a.qs[q];
-    const int t = a.mode == MODE_STCON ? a.qt[q] : s;
+    int s = a.qs[q];
+    int t = a.mode == MODE_STCON ? a.qt[q] : s;
     const int cap = a.exclusive ? nv : min(nv, a.log_cap);
     if (s < 0 || s >= nv || t < 0 || t >= nv) {
         if (tid == 0) {
@@ -454,28 +467,34 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
         __syncthreads();
         return;
     }
+    if (gp.fwd.remap) {  // a renumbered copy of the graph: the caller's ids map into it
+        s = __ldg(gp.fwd.remap + s);
+        t = __ldg(gp.fwd.remap + t);
+    }
     int32_t *levels = a.levels;
+    // the degree histogram is counted only for the learned schedule and traces
+    const bool track = (a.sched == FC_SCHED_LEARNED && a.mlp) || a.trace;
+    // the step description lives in shared memory and only thread 0 reads or
+    // writes it (it is copied to the slot when a step is published)
+    PoolDesc &desc = sm.own;
     if (tid == 0) {
         init_roots(a.mode, gp, s, t, status, levels, log, cap, &my->tc);
         __threadfence();
         ql_start(sm.ql, a.mode == MODE_STCON, nv, gp.fwd.ne, s, t, my->tc.deg[0], my->tc.deg[1]);
         sm.stc = my->tc;
         sm.err = 0;
+        desc.q = q;
+        desc.gidx = gidx;
+        desc.mode = a.mode;
+        desc.cap = cap;
+        desc.status = status;
+        desc.levels = levels;
+        desc.log = log;
+        desc.nreset = 0;
+        desc.split_e = a.split_e;
+        desc.track_hist = track;
     }
     __syncthreads();
-    PoolDesc desc;
-    desc.q = q;
-    desc.gidx = gidx;
-    desc.mode = a.mode;
-    desc.cap = cap;
-    desc.status = status;
-    desc.levels = levels;
-    desc.log = log;
-    desc.nreset = 0;
-    desc.split_e = a.split_e;
-    // the degree histogram is counted only for the learned schedule and traces
-    const bool track = (a.sched == FC_SCHED_LEARNED && a.mlp) || a.trace;
-    desc.track_hist = track;
     const int bu_cap = a.mode == MODE_BFS ? INT_MAX : LEVEL7_MAX;
     while (true) {
         if (tid < 32 && !sm.ql.done) {
@@ -528,18 +547,10 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
         int F;
         const int32_t *front = ql_frontier(sm.ql, log, cap, x, &F);
         if (!sm.publish) {
-            run_step<T>(a.mode, gp, x, DIR_TD, sm.ql.radius[x], sm.ql.radius[1 - x], front, F, 0, 1,
-                        status, levels, log, cap, &sm.stc.tail[x], &sm.stc.deg[x], &sm.stc.found,
-                        &sm.stc.inspected, sm.td, sm.ql.variant, track ? &sm.stc.hist[x] : nullptr);
+            pool_private_step<T>(a.mode, gp, x, sm.ql.radius[x], sm.ql.radius[1 - x], front, F,
+                                 status, levels, log, cap, sm, sm.ql.variant, track);
             __syncthreads();
         } else {
-            desc.side = x;
-            desc.dir = sm.ql.dir;
-            desc.variant = sm.ql.variant;
-            desc.level = sm.ql.radius[x];
-            desc.other_radius = sm.ql.radius[1 - x];
-            desc.F = F;
-            desc.front_off = (int)(front - log);
             // top-down tiles by work: frontiers of high average degree get
             // tiles of fewer vertices (down to one) so that a tile reads
             // about tile_e entries; low-degree frontiers get tiles of T
@@ -557,11 +568,20 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
                 const int want = 8 * (int)gridDim.x;
                 if (chunks > want) tv = T * ((chunks + want - 1) / want);
             }
-            desc.tile_v = tv;
-            const int nvt = desc.dir == DIR_TD ? (int)(((long long)F + tv - 1) / tv)
-                                               : (nv + POOL_TILE_V - 1) / POOL_TILE_V;
-            desc.nvt = nvt;
-            if (tid == 0) counters_to_slot(my, sm.stc);  // published by the fence in the call
+            const int nvt = sm.ql.dir == DIR_TD ? (int)(((long long)F + tv - 1) / tv)
+                                                : (nv + POOL_TILE_V - 1) / POOL_TILE_V;
+            if (tid == 0) {
+                desc.side = x;
+                desc.dir = sm.ql.dir;
+                desc.variant = sm.ql.variant;
+                desc.level = sm.ql.radius[x];
+                desc.other_radius = sm.ql.radius[1 - x];
+                desc.F = F;
+                desc.front_off = (int)(front - log);
+                desc.tile_v = tv;
+                desc.nvt = nvt;
+                counters_to_slot(my, sm.stc);  // published by the fence in the call
+            }
             pool_publish_and_run<T>(a, my, desc, nvt, sm);
             if (sm.err) return;
             if (tid == 0) counters_from_slot(sm.stc, my);
@@ -613,11 +633,14 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
         if (n0 + n1 <= 4 * POOL_TILE_R) {
             clear_claimed(status, log, cap, n0, 0, (long long)n0 + n1, tid, T);
         } else {
-            desc.F = n0;
-            desc.dir = DIR_RESET;
-            desc.nreset = n0 + n1;
-            desc.nvt = (n0 + n1 + POOL_TILE_R - 1) / POOL_TILE_R;
-            pool_publish_and_run<T>(a, my, desc, desc.nvt, sm);
+            const int nvt = (n0 + n1 + POOL_TILE_R - 1) / POOL_TILE_R;
+            if (tid == 0) {
+                desc.F = n0;
+                desc.dir = DIR_RESET;
+                desc.nreset = n0 + n1;
+                desc.nvt = nvt;
+            }
+            pool_publish_and_run<T>(a, my, desc, nvt, sm);
             if (sm.err) return;
         }
     }

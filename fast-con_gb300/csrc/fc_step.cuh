@@ -74,8 +74,33 @@ __device__ __forceinline__ void log_write(const AppendTarget &a, int pos, int v)
         a.log[a.nv - 1 - pos] = v;
 }
 
+// Degree-sum and histogram counters of claims whose degrees d[k] are known:
+// one warp reduction, then one (non-returning) add by lane 0.  All 32 lanes
+// call it.
+template <int K>
+__device__ __forceinline__ void warp_count_degrees(const int (&c)[K], const int (&d)[K],
+                                                   const AppendTarget &a)
+{
+    long long dsum = 0;
+    int h0 = 0, h2 = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        if (c[k] >= 0) {
+            dsum += d[k];
+            h0 += d[k] < 8;
+            h2 += d[k] >= 128;
+        }
+    dsum = warp_sum_ll(dsum);
+    if (lane_id() == 0 && dsum) atomicAdd(a.deg, (unsigned long long)dsum);
+    if (a.hist) {  // uniform: same pointer in every lane
+        const unsigned long long w =
+            (unsigned long long)warp_sum_i(h0) | ((unsigned long long)warp_sum_i(h2) << 32);
+        if (lane_id() == 0 && w) atomicAdd(a.hist, w);
+    }
+}
+
 // Move the warp's buffered claims to the log: one reservation on the tail
-// counter; the claimed vertices' degrees are summed for the schedule.  All 32
+// counter (their degrees were counted when they were buffered).  All 32
 // lanes call it; the buffer is empty afterwards.
 __device__ __forceinline__ void warp_flush(const AppendTarget &a)
 {
@@ -85,45 +110,30 @@ __device__ __forceinline__ void warp_flush(const AppendTarget &a)
     const int *buf = a.wlog + w * WARP_LOG;
     int base = 0;
     if (lane == 0) base = atomicAdd(a.tail, n);
-    int v[WARP_LOG / 32], d[WARP_LOG / 32];
+    base = __shfl_sync(0xffffffffu, base, 0);
 #pragma unroll
     for (int j = 0; j < WARP_LOG / 32; ++j) {
         const int i = j * 32 + lane;
-        v[j] = i < n ? buf[i] : -1;
-        d[j] = v[j] >= 0 ? __ldg(a.row_ptr + v[j] + 1) - __ldg(a.row_ptr + v[j]) : 0;
-    }
-    base = __shfl_sync(0xffffffffu, base, 0);
-    long long dsum = 0;
-    int h0 = 0, h2 = 0;
-#pragma unroll
-    for (int j = 0; j < WARP_LOG / 32; ++j)
-        if (v[j] >= 0) {
-            log_write(a, base + j * 32 + lane, v[j]);
-            dsum += d[j];
-            h0 += d[j] < 8;
-            h2 += d[j] >= 128;
-        }
-    dsum = warp_sum_ll(dsum);
-    if (lane == 0) atomicAdd(a.deg, (unsigned long long)dsum);
-    if (a.hist) {
-        const unsigned long long hw =
-            (unsigned long long)warp_sum_i(h0) | ((unsigned long long)warp_sum_i(h2) << 32);
-        if (lane == 0 && hw) atomicAdd(a.hist, hw);
+        if (i < n) log_write(a, base + i, buf[i]);
     }
     __syncwarp();
     if (lane == 0) a.wcnt[w] = 0;
     __syncwarp();
 }
 
-// All 32 lanes of the warp must call this with the same K.
+// Append the claimed vertices c[k] >= 0, whose degrees in the CSR the side
+// expands next are d[k].  All 32 lanes of the warp must call this with the
+// same K.
 template <int K>
-__device__ __forceinline__ void warp_append(const int (&c)[K], const AppendTarget &a)
+__device__ __forceinline__ void warp_append_deg(const int (&c)[K], const int (&d)[K],
+                                                const AppendTarget &a)
 {
     int cnt = 0;
 #pragma unroll
     for (int k = 0; k < K; ++k) cnt += c[k] >= 0;
     unsigned any = __ballot_sync(0xffffffffu, cnt > 0);
     if (!any) return;
+    warp_count_degrees<K>(c, d, a);
     int incl = warp_inclusive_scan(cnt);
     int total = __shfl_sync(0xffffffffu, incl, 31);
     if (a.wlog && total <= WARP_LOG) {
@@ -143,32 +153,24 @@ __device__ __forceinline__ void warp_append(const int (&c)[K], const AppendTarge
         __syncwarp();
         return;
     }
-    long long dsum = 0;
-    int h0 = 0, h2 = 0;
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-        if (c[k] >= 0) {
-            const int d = __ldg(a.row_ptr + c[k] + 1) - __ldg(a.row_ptr + c[k]);
-            dsum += d;
-            h0 += d < 8;
-            h2 += d >= 128;
-        }
-    dsum = warp_sum_ll(dsum);
     int base = 0;
-    if (lane_id() == 0) {
-        base = atomicAdd(a.tail, total);
-        atomicAdd(a.deg, (unsigned long long)dsum);
-    }
-    if (a.hist) {  // uniform: same pointer in every lane
-        const unsigned long long w =
-            (unsigned long long)warp_sum_i(h0) | ((unsigned long long)warp_sum_i(h2) << 32);
-        if (lane_id() == 0 && w) atomicAdd(a.hist, w);
-    }
+    if (lane_id() == 0) base = atomicAdd(a.tail, total);
     base = __shfl_sync(0xffffffffu, base, 0);
     int pos = base + incl - cnt;
 #pragma unroll
     for (int k = 0; k < K; ++k)
         if (c[k] >= 0) log_write(a, pos++, c[k]);
+}
+
+// The same for claims whose degrees are not known yet: they are read here.
+template <int K>
+__device__ __forceinline__ void warp_append(const int (&c)[K], const AppendTarget &a)
+{
+    int d[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        d[k] = c[k] >= 0 ? __ldg(a.row_ptr + c[k] + 1) - __ldg(a.row_ptr + c[k]) : 0;
+    warp_append_deg<K>(c, d, a);
 }
 
 // ---------------------------------------------------------------------------
@@ -201,6 +203,10 @@ struct VisitSTCON {
         return (uint8_t)(w >> ((unsigned)(v & 3) * 8u));
     }
     __device__ __forceinline__ int probe(int v) const { return (int)__ldcg(word(v)); }
+    __device__ __forceinline__ bool looks_free(int v, int p) const
+    {
+        return byte_of((unsigned)p, v) == ST_UNVISITED;
+    }
     __device__ __forceinline__ int attempt(int v, int p) const
     {
         if (byte_of((unsigned)p, v) != ST_UNVISITED) return p;
@@ -221,6 +227,7 @@ struct VisitBFS {
     int32_t *levels;
     int32_t next_level;
     __device__ __forceinline__ int probe(int v) const { return ld_cg(levels + v); }
+    __device__ __forceinline__ bool looks_free(int, int p) const { return p < 0; }
     __device__ __forceinline__ int attempt(int v, int p) const
     {
         return p >= 0 ? p : atomicCAS(levels + v, -1, next_level);
@@ -244,9 +251,41 @@ __device__ __forceinline__ void visit_k(const Vis &vis, const int (&v)[K], int (
     for (int k = 0; k < K; ++k) c[k] = v[k] >= 0 ? vis.resolve(v[k], r[k]) : -1;
 }
 
+// The same, and the degrees d[k] (in the CSR `rp` the side expands next) of
+// the claimed vertices: the row range of every neighbour whose probe found it
+// free is read together with its claim, so the degree costs no round trip
+// of its own after the claim returns.  A neighbour that another thread
+// claims first costs two loads for nothing; the probe keeps those rare.
+template <int K, class Vis>
+__device__ __forceinline__ void visit_k_deg(const Vis &vis, const int32_t *__restrict__ rp,
+                                            const int (&v)[K], int (&c)[K], int (&d)[K])
+{
+    int r[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) r[k] = v[k] >= 0 ? vis.probe(v[k]) : 0;
+    int rb[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const bool f = v[k] >= 0 && vis.looks_free(v[k], r[k]);
+        rb[k] = f ? __ldg(rp + v[k]) : 0;
+        d[k] = f ? __ldg(rp + v[k] + 1) : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) r[k] = v[k] >= 0 ? vis.attempt(v[k], r[k]) : 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        c[k] = v[k] >= 0 ? vis.resolve(v[k], r[k]) : -1;
+        d[k] -= rb[k];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Walk col[b, e) with `nlanes` threads (lane_idx in [0, nlanes)); every warp
-// of the group must call it (loop trip counts are uniform per warp).
+// of the group must call it (loop trip counts are uniform per warp).  The
+// aligned middle is read with two 16-byte loads per lane and round; the at
+// most 6 unaligned entries at the ends are scalar loads of the group's first
+// lanes that join the first round, so a row costs one dependent chain of
+// loads, probes and claims per round and no extra one for its ends.
 // ---------------------------------------------------------------------------
 template <class Vis>
 __device__ __forceinline__ void walk_range(const int32_t *__restrict__ col, int b, int e,
@@ -254,23 +293,19 @@ __device__ __forceinline__ void walk_range(const int32_t *__restrict__ col, int 
                                            const AppendTarget &app)
 {
     if (app.reads && lane_idx == 0 && e > b) atomicAdd(app.reads, (unsigned long long)(e - b));
-    int a = min((b + 3) & ~3, e);
-    int z = max(e & ~3, a);
-    int nhead = a - b, ntail = e - z;
-    if (nhead + ntail > 0 && lane_idx < 32) {
-        // at most 6 scalar entries: only the group's first warp takes part
-        int c[1] = {-1};
-        if (lane_idx < nhead)
-            c[0] = vis.visit(__ldg(col + b + lane_idx));
-        else if (lane_idx < nhead + ntail)
-            c[0] = vis.visit(__ldg(col + z + lane_idx - nhead));
-        warp_append<1>(c, app);
-    }
-    // two 16-byte loads per lane and round: 8 neighbours' probes in flight
+    const int a = min((b + 3) & ~3, e);
+    const int z = max(e & ~3, a);
+    const int nhead = a - b, ntail = e - z;
+    int hv = -1;
+    if (lane_idx < nhead)
+        hv = __ldg(col + b + lane_idx);
+    else if (lane_idx < nhead + ntail)
+        hv = __ldg(col + z + lane_idx - nhead);
     const int4 *col4 = reinterpret_cast<const int4 *>(col);
     const int k_end = z >> 2;
-    for (int k0 = a >> 2; k0 < k_end; k0 += 2 * nlanes) {
-        int v[8], c[8];
+    int k0 = a >> 2;
+    do {  // at least one round: it carries the scalar ends
+        int v[9], c[9];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int k = k0 + h * nlanes + lane_idx;
@@ -281,9 +316,12 @@ __device__ __forceinline__ void walk_range(const int32_t *__restrict__ col, int 
             v[4 * h + 2] = x.z;
             v[4 * h + 3] = x.w;
         }
-        visit_k<8>(vis, v, c);
-        warp_append<8>(c, app);
-    }
+        v[8] = hv;
+        hv = -1;
+        visit_k<9>(vis, v, c);
+        warp_append<9>(c, app);
+        k0 += 2 * nlanes;
+    } while (k0 < k_end);
 }
 
 template <int T>
@@ -419,45 +457,50 @@ __device__ __forceinline__ void expand_lb(const int32_t *__restrict__ col, int r
 // ---------------------------------------------------------------------------
 // Variant 1, warp-centric: the warp expands the rows of its 32 lanes without
 // any CTA barrier.  Rows longer than `big` go to the sink (row jobs) when it
-// takes them; rows of >= 32 entries are walked by the whole warp; shorter
-// rows are flattened by a warp prefix scan, and each lane finds the row of
-// its edge by a 5-step shuffle search over the scan.
+// takes them.  The remaining rows are laid end to end by a warp prefix scan
+// and read GATHER_PER_THREAD entries per lane and round (256 per round, the
+// lanes of a row on consecutive entries); each lane finds the row of an
+// entry by a 5-step shuffle search over the scan.  A frontier of a few long
+// rows and many short ones thus costs ceil(entries / 256) dependent rounds,
+// not one round per long row plus one per 32 short-row entries.
 // ---------------------------------------------------------------------------
-template <class Vis, class Sink>
+template <class Vis, class Sink, bool SPEC_DEG = false>
 __device__ __forceinline__ void expand_warp(const int32_t *__restrict__ col, int rb, int re,
                                             const Vis &vis, const AppendTarget &app,
                                             const Sink &sink, int big)
 {
+    constexpr int K = GATHER_PER_THREAD;
     const int lane = (int)lane_id();
     if (re - rb > big && sink.push_row(rb, re)) rb = re;
-    while (true) {
-        unsigned m = __ballot_sync(0xffffffffu, re - rb >= 32);
-        if (!m) break;
-        int leader = __ffs(m) - 1;
-        int b = __shfl_sync(0xffffffffu, rb, leader);
-        int e = __shfl_sync(0xffffffffu, re, leader);
-        if (lane == leader) rb = re;
-        walk_range(col, b, e, lane, 32, vis, app);
-    }
     const int d = re - rb;
     const int incl = warp_inclusive_scan(d);
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     const int excl = incl - d;
     if (app.reads && lane == 0 && total > 0) atomicAdd(app.reads, (unsigned long long)total);
-    for (int base = 0; base < total; base += 32) {
-        const int e = base + lane;
-        int pos = 0;  // number of lanes whose rows end at or before edge e
+    for (int base = 0; base < total; base += 32 * K) {
+        int v[K], c[K];
 #pragma unroll
-        for (int s = 16; s > 0; s >>= 1) {
-            int v = __shfl_sync(0xffffffffu, incl, pos + s - 1);
-            if (v <= e) pos += s;
+        for (int j = 0; j < K; ++j) {
+            const int e = base + j * 32 + lane;
+            int pos = 0;  // number of lanes whose rows end at or before entry e
+#pragma unroll
+            for (int s = 16; s > 0; s >>= 1) {
+                const int w = __shfl_sync(0xffffffffu, incl, pos + s - 1);
+                if (w <= e) pos += s;
+            }
+            const int owner = pos < 32 ? pos : 31;
+            const int ob = __shfl_sync(0xffffffffu, rb, owner);
+            const int oe = __shfl_sync(0xffffffffu, excl, owner);
+            v[j] = e < total ? __ldg(col + ob + (e - oe)) : -1;
         }
-        const int owner = pos < 32 ? pos : 31;
-        const int ob = __shfl_sync(0xffffffffu, rb, owner);
-        const int oe = __shfl_sync(0xffffffffu, excl, owner);
-        int c[1] = {-1};
-        if (e < total) c[0] = vis.visit(__ldg(col + ob + (e - oe)));
-        warp_append<1>(c, app);
+        if constexpr (SPEC_DEG) {
+            int dg[K];
+            visit_k_deg<K>(vis, app.row_ptr, v, c, dg);
+            warp_append_deg<K>(c, dg, app);
+        } else {
+            visit_k<K>(vis, v, c);
+            warp_append<K>(c, app);
+        }
     }
 }
 
@@ -550,7 +593,7 @@ __device__ void topdown_step(const int32_t *__restrict__ row_ptr, const int32_t 
             re = __ldg(row_ptr + u + 1);
         }
         if (warp_sum_i(re - rb) <= TINY_STEP_E) {
-            if (tid < 32) expand_warp(col, rb, re, vis, app, NoSink{}, INT_MAX);
+            if (tid < 32) expand_warp<Vis, NoSink, true>(col, rb, re, vis, app, NoSink{}, INT_MAX);
             return;
         }
     }
