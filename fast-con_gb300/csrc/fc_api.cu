@@ -77,17 +77,23 @@ int ensure_layout(fc_graph *g, int order, cudaStream_t st)
     return FC_OK;
 }
 
-// The graph a batch runs on.  On the batched engine an undirected graph with
-// hubs is searched in its degree-ordered copy: the hubs' status bytes then
-// share a few sectors of each query slot, which stay in L2, instead of one
-// sector per hub anywhere in the slot (R-MAT 24, 1,024 queries: 0.39 ->
-// 0.28 ms).  The kernels map s and t through the copy's id map; answers do
-// not depend on the numbering.  Directed graphs keep theirs (the copy holds
-// no reverse CSR).  The caller holds the device lock.
-int batch_pair(fc_graph *g, const fc_opts &o, cudaStream_t st, fc::GraphPairH *p)
+// The graph an s-t search runs on.  An undirected graph with hubs is searched
+// in its degree-ordered copy: the hubs' status bytes then share a few
+// sectors of each query's status array, which stay in L2, instead of one
+// sector per hub anywhere in it (R-MAT 24, a batch of 1,024 queries: 0.39 ->
+// 0.26 ms).  The kernels map s and t through the copy's id map; answers
+// (connected, hop distance) do not depend on the numbering.  Directed graphs
+// keep theirs (the copy holds no reverse CSR), and so does the host-loop
+// engine, whose host side reads the ids.  A single query (batch = 0) uses
+// the copy only when asked (FC_ORDER_DEGREE): alone on the GPU its status
+// array stays in L2 anyway, and on the copy the grid's claims crowd the few
+// words that hold the hubs (R-MAT 24: 0.096 -> 0.106 ms per query).  The
+// caller holds the device lock.
+int search_pair(fc_graph *g, const fc_opts &o, int batch, cudaStream_t st, fc::GraphPairH *p)
 {
     *p = pair_of(g);
-    if (g->directed || !(o.engine == FC_ENGINE_AUTO || o.engine == FC_ENGINE_BATCHED)) return FC_OK;
+    if (g->directed || o.engine == FC_ENGINE_HOSTLOOP) return FC_OK;
+    if (!batch && o.vertex_order != FC_ORDER_DEGREE) return FC_OK;
     int rc = ensure_layout(g, o.vertex_order, st);
     if (rc) return rc;
     if (o.vertex_order != FC_ORDER_GIVEN && g->bfs_layout) {
@@ -552,7 +558,10 @@ int fc_stcon_ex(fc_graph *g, int32_t s, int32_t t, int32_t *connected, int32_t *
     fc_opts o = opts ? *opts : default_opts();
     CtxLock L;
     if (!L.c) return L.rc;
-    return fc::engine_stcon(L.c, pair_of(g), s, t, connected, hops, o, stats, pick_stream(opts, L.c));
+    fc::GraphPairH p;
+    int rc = search_pair(g, o, 0, pick_stream(opts, L.c), &p);
+    if (rc) return rc;
+    return fc::engine_stcon(L.c, p, s, t, connected, hops, o, stats, pick_stream(opts, L.c));
 }
 
 int fc_stcon(fc_graph *g, int32_t s, int32_t t, int32_t *connected, int32_t *hops)
@@ -587,7 +596,7 @@ int fc_stcon_batch_device(fc_graph *const *gs, int32_t ngraphs, const int32_t *d
     if (!L.c) return L.rc;
     std::vector<fc::GraphPairH> pairs((size_t)ngraphs);
     for (int i = 0; i < ngraphs; ++i) {
-        int rc = batch_pair(gs[i], o, pick_stream(opts, L.c), &pairs[(size_t)i]);
+        int rc = search_pair(gs[i], o, 1, pick_stream(opts, L.c), &pairs[(size_t)i]);
         if (rc) return rc;
     }
     return fc::engine_stcon_batch(L.c, pairs.data(), ngraphs, d_graph_idx, d_s, d_t, nq, d_connected,
@@ -620,7 +629,7 @@ int fc_autotune_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *d_gra
         fc_opts ob = *inout;
         ob.engine = FC_ENGINE_BATCHED;
         for (int i = 0; i < ngraphs; ++i) {
-            int rc = batch_pair(gs[i], ob, st, &pairs[(size_t)i]);
+            int rc = search_pair(gs[i], ob, 1, st, &pairs[(size_t)i]);
             if (rc) return rc;
         }
     }
@@ -693,7 +702,7 @@ int fc_stcon_batch_scripted(fc_graph *g, const int32_t *d_s, const int32_t *d_t,
     ex.trace_count = d_trace_count;
     ex.inspected = reinterpret_cast<long long *>(d_inspected);
     fc::GraphPairH p;
-    int rc = batch_pair(g, o, st, &p);
+    int rc = search_pair(g, o, 1, st, &p);
     if (rc) {
         cudaFreeAsync(dc, st);
         return rc;
@@ -834,7 +843,7 @@ int fc_stcon_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *graph_id
     fc_opts o = opts ? *opts : default_opts();
     std::vector<fc::GraphPairH> pairs((size_t)ngraphs);
     for (int i = 0; i < ngraphs; ++i) {
-        rc = batch_pair(gs[i], o, st, &pairs[(size_t)i]);
+        rc = search_pair(gs[i], o, 1, st, &pairs[(size_t)i]);
         if (rc) return rc;
     }
     // the answers' copies and the engine's error words travel together, so

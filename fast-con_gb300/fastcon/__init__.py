@@ -170,8 +170,10 @@ def make_opts(sched=SCHED_HEURISTIC, engine=ENGINE_AUTO, block=0, ctas_per_sm=0,
               job_entries=0, private_variant=0, vertex_order=0) -> Opts:
     """variant: 0 = chosen by the schedule, 1 hybrid, 2 warp-centric, 3 lane per row;
     tile_entries / job_entries: work-sharing tile and row-job sizes (0 = defaults);
-    vertex_order: numbering of the plain BFS engine (ORDER_AUTO / ORDER_GIVEN /
-    ORDER_DEGREE)."""
+    vertex_order: numbering the search runs on (ORDER_AUTO / ORDER_GIVEN /
+    ORDER_DEGREE): the plain BFS engine and s-t batches of undirected graphs
+    (single queries only with ORDER_DEGREE); ids in and levels out are always
+    the caller's."""
     o = Opts()
     lib().fc_opts_init(ctypes.byref(o))
     o.sched, o.engine, o.block, o.ctas_per_sm = sched, engine, block, ctas_per_sm

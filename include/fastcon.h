@@ -83,12 +83,22 @@ typedef struct fc_opts {
     int32_t private_variant; /* work-sharing engine: expansion variant of the
                              steps an owner CTA runs alone (same codes as
                              `variant`; 0 = the schedule's choice)          */
-    int32_t vertex_order; /* plain BFS engine (FC_ENGINE_AUTO with
-                             FC_SCHED_PLAIN in fc_bfs_levels_ex): FC_ORDER_* */
+    int32_t vertex_order; /* numbering the search runs on, FC_ORDER_*: the
+                             plain BFS engine (FC_ENGINE_AUTO with
+                             FC_SCHED_PLAIN in fc_bfs_levels_ex) and s-t
+                             batches of undirected graphs (not on the
+                             host-loop engine); single s-t queries use the
+                             copy only with FC_ORDER_DEGREE.  Ids in and
+                             levels out are always the caller's.           */
     int32_t reserved[2];
 } fc_opts;
 
-/* ---- vertex numbering of the plain BFS engine ---------------------------- */
+/* ---- vertex numbering of the searches ------------------------------------ */
+/* The degree-ordered copy (vertices renumbered by descending degree class) is
+ * built by the first search that uses it and kept by the graph handle: as
+ * much device memory again as the CSR, plus an id map.  It packs the hubs'
+ * visited state into a few cache sectors per query slot; a batch of 1,024
+ * s-t queries on R-MAT scale 24 runs about a third faster on it. */
 #define FC_ORDER_AUTO   0  /* degree-ordered copy when the graph has hubs
                               (a vertex of degree >= 256), else as given      */
 #define FC_ORDER_GIVEN  1  /* search the caller's numbering                   */

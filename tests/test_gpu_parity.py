@@ -567,3 +567,48 @@ def test_plain_bfs_engine(fastcon_lib, oracle_mod):
                 assert st["edges_inspected"] == int(deg[want >= 0].sum()), (name, order, src)
                 assert st["alg_bytes"] == 20 * reached - 8 + 8 * st["edges_inspected"]
         G.free()
+
+
+# --------------------------------------------------------------------------
+# s-t searches run on the degree-ordered copy of an undirected graph with
+# hubs unless the caller keeps its numbering: every engine and order gives
+# the oracle's answers, single queries and batches, on graphs with and
+# without hubs (the copy is built only when there are hubs, or when asked)
+# --------------------------------------------------------------------------
+def test_stcon_vertex_order(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    cases = []
+    u, v = graphs.rmat_edges(16, 8 << 16, seed=61, perm_seed=62)
+    cases.append(("rmat16", 1 << 16, u, v))
+    rng = np.random.default_rng(64)
+    u = rng.integers(0, 30000, 90000).astype(np.int32)  # no vertex of degree 256
+    v = rng.integers(0, 30000, 90000).astype(np.int32)
+    cases.append(("er", 30001, u, v))
+    for name, nv, u, v in cases:
+        G = fc.Graph.from_edges(u, v, nv)
+        rp, col = G.csr()
+        deg = np.diff(rp)
+        s, t = graphs.pairs_with_degree(deg, 1200, seed=63)
+        s[1] = t[1] = int(np.argmax(deg))  # s == t on a hub
+        isolated = np.where(deg == 0)[0]
+        s[2] = int(isolated[0]) if len(isolated) else s[2]
+        _, want, _ = oracle_mod.stcon_batch(rp, col, s, t, nthreads=16)
+        for order in (fc.ORDER_AUTO, fc.ORDER_GIVEN, fc.ORDER_DEGREE):
+            for eng in (fc.ENGINE_AUTO, fc.ENGINE_BATCHED, fc.ENGINE_PERSISTENT):
+                for sch in (fc.SCHED_PLAIN, fc.SCHED_HEURISTIC):
+                    o = fc.make_opts(sched=sch, engine=eng, vertex_order=order)
+                    conn, hops = fc.stcon_batch(G, s, t, opts=o)
+                    assert (hops == want).all(), (name, order, eng, sch)
+                    assert (conn == (want >= 0)).all()
+                    for k in (0, 1, 2, 3, 500, 1199):
+                        assert G.stcon(s[k], t[k], o) == (want[k] >= 0, want[k]), (name, k)
+            # the batch's device form (the benchmark's call) with a replayed graph
+            o = fc.make_opts(sched=fc.SCHED_LEARNED, engine=fc.ENGINE_BATCHED, use_graph=1,
+                             vertex_order=order)
+            for _ in range(2):
+                conn, hops = fc.stcon_batch(G, s, t, opts=o)
+                assert (hops == want).all(), (name, order, "graph replay")
+        # the levels of a full BFS are indexed by the caller's ids whatever the order
+        lev, _ = oracle_mod.bfs_levels(rp, col, int(s[0]))
+        assert (G.bfs_levels(int(s[0])) == lev).all()
+        G.free()
