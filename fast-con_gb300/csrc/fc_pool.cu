@@ -477,11 +477,17 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
     // the step description lives in shared memory and only thread 0 reads or
     // writes it (it is copied to the slot when a step is published)
     PoolDesc &desc = sm.own;
+    // thread 0's copy of the query counter, read a step ahead so that the
+    // test for the batch's tail waits on no load of its own
+    int next_seen = 0;
     if (tid == 0) {
-        init_roots(a.mode, gp, s, t, status, levels, log, cap, &my->tc);
-        __threadfence();
-        ql_start(sm.ql, a.mode == MODE_STCON, nv, gp.fwd.ne, s, t, my->tc.deg[0], my->tc.deg[1]);
-        sm.stc = my->tc;
+        if (!a.exclusive) next_seen = ld_cg(&a.ctr[CTR_NEXT]);
+        // the roots and the counters start in this CTA: the counters in
+        // shared memory (the slot's copy is written when a step is
+        // published), the roots' status and log entries read by this CTA
+        // after the barrier below, or by helpers after the publishing fence
+        init_roots(a.mode, gp, s, t, status, levels, log, cap, &sm.stc);
+        ql_start(sm.ql, a.mode == MODE_STCON, nv, gp.fwd.ne, s, t, sm.stc.deg[0], sm.stc.deg[1]);
         sm.err = 0;
         desc.q = q;
         desc.gidx = gidx;
@@ -533,7 +539,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
                 }
                 // in the batch's tail (every query taken, idle CTAs about)
                 // smaller steps are shared, in smaller tiles
-                sm.tail = !a.exclusive && ld_cg(&a.ctr[CTR_NEXT]) >= sm.nq;
+                sm.tail = !a.exclusive && next_seen >= sm.nq;
                 const long long priv = sm.tail ? a.private_edges / 8 : a.private_edges;
                 sm.publish = sm.ql.dir == DIR_BU || m > priv;
                 if (!sm.publish && a.private_variant >= 0 && a.force_variant < 0)
@@ -587,6 +593,7 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             if (tid == 0) counters_from_slot(sm.stc, my);
         }
         if (tid == 0) {
+            if (!a.exclusive && next_seen < sm.nq) next_seen = ld_cg(&a.ctr[CTR_NEXT]);
             const unsigned long long ins0 = sm.ql.inspected;
             const int tail0 = sm.ql.tail[x], F0 = sm.ql.tail[x] - sm.ql.head[x];
             const int dir0 = sm.ql.dir, var0 = sm.ql.variant, step0 = sm.ql.steps;
@@ -644,11 +651,10 @@ __device__ void pool_query(const PoolArgs &a, PoolSlot *my, int q, uint8_t *stat
             if (sm.err) return;
         }
     }
+    // the finished count only tells idle CTAs when to leave: the answers
+    // are read after the kernel ends, so no fence is needed before it
     __syncthreads();
-    if (tid == 0) {
-        __threadfence();
-        atomicAdd(&a.ctr[CTR_FINISHED], 1);
-    }
+    if (tid == 0) atomicAdd(&a.ctr[CTR_FINISHED], 1);
     __syncthreads();
 }
 
