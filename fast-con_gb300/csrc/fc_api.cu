@@ -60,6 +60,18 @@ fc::GraphPairH pair_of(const fc_graph *g)
     return p;
 }
 
+// True when p points into page-locked host memory (cudaMallocHost,
+// cudaHostRegister): only such memory may be copied inside a CUDA graph.
+bool page_locked(const void *p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // pageable memory of an older runtime: not an error
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
 // The degree-ordered copy of g (vertices renumbered by descending degree
 // class), built on first use and kept by the handle: order FC_ORDER_AUTO
 // builds it only for graphs with hubs, FC_ORDER_DEGREE always, and
@@ -837,22 +849,36 @@ int fc_stcon_batch(fc_graph *const *gs, int32_t ngraphs, const int32_t *graph_id
     int32_t *buf = fc::batch_staging(L.c, k, &rc);
     if (!buf) return rc;
     int32_t *ds = buf, *dt = buf + k, *dg = buf + 2 * k, *dc = buf + 3 * k, *dh = buf + 4 * k;
-    FC_CUDA_TRY(cudaMemcpyAsync(ds, s, sizeof(int32_t) * k, cudaMemcpyHostToDevice, st));
-    FC_CUDA_TRY(cudaMemcpyAsync(dt, t, sizeof(int32_t) * k, cudaMemcpyHostToDevice, st));
-    if (graph_idx) FC_CUDA_TRY(cudaMemcpyAsync(dg, graph_idx, sizeof(int32_t) * k, cudaMemcpyHostToDevice, st));
     fc_opts o = opts ? *opts : default_opts();
     std::vector<fc::GraphPairH> pairs((size_t)ngraphs);
     for (int i = 0; i < ngraphs; ++i) {
         rc = search_pair(gs[i], o, 1, st, &pairs[(size_t)i]);
         if (rc) return rc;
     }
-    // the answers' copies and the engine's error words travel together, so
-    // the call waits once
-    rc = fc::engine_stcon_batch(L.c, pairs.data(), ngraphs, graph_idx ? dg : nullptr, ds, dt, nq,
-                                dc, dh, o, stats, st, fc::BATCH_DEFER_CHECK);
-    if (rc == FC_OK) {
-        FC_CUDA_TRY(cudaMemcpyAsync(connected, dc, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, st));
-        FC_CUDA_TRY(cudaMemcpyAsync(hops, dh, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, st));
+    // Page-locked arrays on the batched engine: the engine queues the copies
+    // in and out with its kernels (in its CUDA graph when opts.use_graph is
+    // set).  Otherwise the copies are queued here.  Either way the answers'
+    // copies and the engine's error words travel together and the call
+    // waits once.
+    const bool batched = o.engine == FC_ENGINE_AUTO || o.engine == FC_ENGINE_BATCHED;
+    const bool locked = batched && page_locked(s) && page_locked(t) &&
+                        (!graph_idx || page_locked(graph_idx)) && page_locked(connected) &&
+                        page_locked(hops);
+    if (locked) {
+        const fc::BatchHostIO hio{s, t, graph_idx, connected, hops};
+        rc = fc::engine_stcon_batch(L.c, pairs.data(), ngraphs, graph_idx ? dg : nullptr, ds, dt,
+                                    nq, dc, dh, o, stats, st, fc::BATCH_DEFER_CHECK, nullptr, &hio);
+    } else {
+        FC_CUDA_TRY(cudaMemcpyAsync(ds, s, sizeof(int32_t) * k, cudaMemcpyHostToDevice, st));
+        FC_CUDA_TRY(cudaMemcpyAsync(dt, t, sizeof(int32_t) * k, cudaMemcpyHostToDevice, st));
+        if (graph_idx)
+            FC_CUDA_TRY(cudaMemcpyAsync(dg, graph_idx, sizeof(int32_t) * k, cudaMemcpyHostToDevice, st));
+        rc = fc::engine_stcon_batch(L.c, pairs.data(), ngraphs, graph_idx ? dg : nullptr, ds, dt,
+                                    nq, dc, dh, o, stats, st, fc::BATCH_DEFER_CHECK);
+        if (rc == FC_OK) {
+            FC_CUDA_TRY(cudaMemcpyAsync(connected, dc, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, st));
+            FC_CUDA_TRY(cudaMemcpyAsync(hops, dh, sizeof(int32_t) * k, cudaMemcpyDeviceToHost, st));
+        }
     }
     // the staging buffer is reused by the next call
     cudaStreamSynchronize(st);

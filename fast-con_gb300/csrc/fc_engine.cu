@@ -335,11 +335,18 @@ static int ensure_graphs(DevCtx *c, const GraphPairH *gps, int n, cudaStream_t s
         cudaFree(c->d_graphs);
         c->d_graphs = nullptr;
         c->graphs_cap = 0;
+        c->graphs_last.clear();
         FC_CUDA_TRY(cudaMalloc(&c->d_graphs, sizeof(GraphPair) * (size_t)n));
         c->graphs_cap = (size_t)n;
     }
-    FC_CUDA_TRY(cudaMemcpyAsync(c->d_graphs, gps, sizeof(GraphPair) * (size_t)n,
-                                cudaMemcpyHostToDevice, st));
+    // repeated batches on the same graphs (the common case) skip the copy
+    const size_t bytes = sizeof(GraphPair) * (size_t)n;
+    if (c->graphs_last.size() == bytes && std::memcmp(c->graphs_last.data(), gps, bytes) == 0)
+        return FC_OK;
+    c->graphs_last.clear();
+    FC_CUDA_TRY(cudaMemcpyAsync(c->d_graphs, gps, bytes, cudaMemcpyHostToDevice, st));
+    c->graphs_last.assign(reinterpret_cast<const unsigned char *>(gps),
+                          reinterpret_cast<const unsigned char *>(gps) + bytes);
     return FC_OK;
 }
 
@@ -840,8 +847,13 @@ static int ensure_batch_arena(DevCtx *c, size_t slots, size_t maxnv, int log_cap
 int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int32_t *d_gi,
                        const int32_t *d_s, const int32_t *d_t, int32_t nq, int32_t *d_conn,
                        int32_t *d_hops, const fc_opts &o, fc_stats *st, cudaStream_t stream,
-                       int check, const BatchExtras *ex)
+                       int check, const BatchExtras *ex, const BatchHostIO *hio)
 {
+    if (hio && pick_engine(o, FC_ENGINE_BATCHED) != FC_ENGINE_BATCHED) {
+        set_error("host arrays are copied by the batched engine only");
+        return FC_ERR_UNSUPPORTED;
+    }
+    const bool hio_checks = hio && check == BATCH_DEFER_CHECK && !st;
     constexpr int T = FC_BLOCK;
     c->deferred_engine = -1;
     if (nq <= 0) return FC_OK;
@@ -951,22 +963,50 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         x.jobs = c->tjobs;
         x.jcap = c->tjobs_cap;
         const int xgrid = coop_grid<T>(c);
+        const size_t qb = sizeof(int32_t) * (size_t)nq;
         auto issue = [&](unsigned evflags) -> int {
+            if (hio) {
+                FC_CUDA_TRY(cudaMemcpyAsync((void *)d_s, hio->s, qb, cudaMemcpyHostToDevice, stream));
+                FC_CUDA_TRY(cudaMemcpyAsync((void *)d_t, hio->t, qb, cudaMemcpyHostToDevice, stream));
+                if (hio->gi)
+                    FC_CUDA_TRY(cudaMemcpyAsync((void *)d_gi, hio->gi, qb, cudaMemcpyHostToDevice,
+                                                stream));
+            }
             FC_CUDA_TRY(cudaMemsetAsync(c->qstat, 0, sizeof(QueryStat) * (size_t)nq, stream));
             FC_CUDA_TRY(cudaMemsetAsync(c->b_ctr, 0, 8 * sizeof(int), stream));
             int r = pool_launch(a, grid, block, stream);
             if (r) return r;
             FC_CUDA_TRY(cudaEventRecordWithFlags(c->evm, stream, evflags));
-            return launch_persistent<T>(c, x, stream);
+            r = launch_persistent<T>(c, x, stream);
+            if (r) return r;
+            if (hio) {
+                if (hio_checks) {  // the error words travel with the answers
+                    FC_CUDA_TRY(cudaMemcpyAsync(c->h_bctr, c->b_ctr, 8 * sizeof(int),
+                                                cudaMemcpyDeviceToHost, stream));
+                    FC_CUDA_TRY(cudaMemcpyAsync(c->h_tc, c->tc, sizeof(TeamCounters),
+                                                cudaMemcpyDeviceToHost, stream));
+                }
+                FC_CUDA_TRY(cudaMemcpyAsync(hio->conn, d_conn, qb, cudaMemcpyDeviceToHost, stream));
+                FC_CUDA_TRY(cudaMemcpyAsync(hio->hops, d_hops, qb, cudaMemcpyDeviceToHost, stream));
+            }
+            return FC_OK;
         };
         if (o.use_graph) {
             // the two launches and their resets as one CUDA graph, replayed
             // while every argument (pointers, sizes, grids) stays the same
-            unsigned char key[sizeof(PoolArgs) + sizeof(PersistArgs) + 4 * sizeof(int)];
+            // (the host arrays' addresses and whether the error words are
+            // copied are part of the graph too)
+            BatchHostIO hk;
+            std::memset(&hk, 0, sizeof(hk));
+            if (hio) hk = *hio;
+            unsigned char key[sizeof(PoolArgs) + sizeof(PersistArgs) + 5 * sizeof(int) +
+                              sizeof(BatchHostIO)];
             std::memcpy(key, &a, sizeof(PoolArgs));
             std::memcpy(key + sizeof(PoolArgs), &x, sizeof(PersistArgs));
-            int tail[4] = {grid, xgrid, nq, block};
+            int tail[5] = {grid, xgrid, nq, block, (hio ? 1 : 0) | (hio_checks ? 2 : 0)};
             std::memcpy(key + sizeof(PoolArgs) + sizeof(PersistArgs), tail, sizeof(tail));
+            std::memcpy(key + sizeof(PoolArgs) + sizeof(PersistArgs) + sizeof(tail), &hk,
+                        sizeof(hk));
             static_assert(sizeof(key) <= sizeof(c->gkey), "graph key too large");
             if (!(c->gexec && c->gkey_len == sizeof(key) &&
                   std::memcmp(c->gkey, key, sizeof(key)) == 0)) {
@@ -1073,6 +1113,10 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
         return FC_ERR_UNSUPPORTED;
     }
     FC_CUDA_TRY(cudaEventRecord(c->ev1, stream));
+    if (hio_checks) {  // queued with the answers
+        c->deferred_engine = engine;
+        return FC_OK;
+    }
     if (check == BATCH_DEFER_CHECK && !st) {
         if (engine != FC_ENGINE_PERSISTENT)
             FC_CUDA_TRY(cudaMemcpyAsync(c->h_bctr, c->b_ctr, 8 * sizeof(int),

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <mutex>
+#include <vector>
 
 #include "fastcon.h"
 
@@ -53,6 +54,7 @@ struct DevCtx {
     TeamCounters *h_tc = nullptr;    // pinned mirror
     void *d_graphs = nullptr;        // GraphPair table
     size_t graphs_cap = 0;
+    std::vector<unsigned char> graphs_last;  // the table's last upload (host copy)
     // batched arena
     uint8_t *b_status = nullptr;
     int32_t *b_log = nullptr;
@@ -82,7 +84,7 @@ struct DevCtx {
     cudaStream_t stream = nullptr;
     // cached CUDA graph of the last batched launch, keyed by its arguments
     cudaGraphExec_t gexec = nullptr;
-    unsigned char gkey[512];
+    unsigned char gkey[640];
     size_t gkey_len = 0;
     int graph_replays = 0;           // replays of the cached graph (tests)
     int graph_captures = 0;          // captures made
@@ -144,10 +146,19 @@ struct BatchExtras {
 // stream (one wait for the results and the checks together).  Statistics
 // (st != nullptr) always wait.
 constexpr int BATCH_NO_CHECK = 0, BATCH_CHECK = 1, BATCH_DEFER_CHECK = 2;
+// Page-locked host arrays of a host-array batch on the batched engine: the
+// engine copies s, t (and gi) into its device arguments before the kernels
+// and the answers (and, with BATCH_DEFER_CHECK, the error words) back after
+// them, all inside the batch's CUDA graph when one is used.
+struct BatchHostIO {
+    const int32_t *s, *t, *gi;  // gi nullable
+    int32_t *conn, *hops;
+};
 int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int32_t *d_gi,
                        const int32_t *d_s, const int32_t *d_t, int32_t nq, int32_t *d_conn,
                        int32_t *d_hops, const fc_opts &o, fc_stats *st, cudaStream_t stream,
-                       int check, const BatchExtras *ex = nullptr);
+                       int check, const BatchExtras *ex = nullptr,
+                       const BatchHostIO *hio = nullptr);
 // The error words a BATCH_DEFER_CHECK call queued, read after the stream was
 // synchronised: FC_OK, or FC_ERR_TIMEOUT with the workspaces reset.
 int engine_finish_checks(DevCtx *c);

@@ -612,3 +612,55 @@ def test_stcon_vertex_order(fastcon_lib, oracle_mod):
         lev, _ = oracle_mod.bfs_levels(rp, col, int(s[0]))
         assert (G.bfs_levels(int(s[0])) == lev).all()
         G.free()
+
+
+# --------------------------------------------------------------------------
+# host-array batches from page-locked memory: the engine copies the queries
+# in and the answers out with its kernels, inside the captured CUDA graph
+# when one is used; new contents of the same arrays are read on replay
+# --------------------------------------------------------------------------
+def test_batch_page_locked_host_arrays(fastcon_lib, oracle_mod):
+    import torch
+    fc = fastcon_lib
+    gs, csrs = [], []
+    for k, sc in enumerate((12, 14)):
+        u, v = graphs.rmat_edges(sc, 8 << sc, seed=90 + k, perm_seed=91 + k)
+        G = fc.Graph.from_edges(u, v, 1 << sc)
+        gs.append(G)
+        csrs.append(G.csr())
+    nq = 700
+    rng = np.random.default_rng(92)
+
+    def pinned(a):
+        return torch.from_numpy(np.ascontiguousarray(a, dtype=np.int32)).pin_memory().numpy()
+
+    hs, ht, hg = pinned(np.zeros(nq)), pinned(np.zeros(nq)), pinned(np.zeros(nq))
+    hc, hh = pinned(np.full(nq, -7)), pinned(np.full(nq, -7))
+    for use_graph in (1, 0):
+        for sch in (fc.SCHED_HEURISTIC, fc.SCHED_LEARNED):
+            o = fc.make_opts(sched=sch, engine=fc.ENGINE_BATCHED, use_graph=use_graph)
+            for rep in range(3):  # new queries in the same arrays each call
+                hg[:] = rng.integers(0, 2, nq)
+                for j in range(nq):
+                    n = 1 << (12 if hg[j] == 0 else 14)
+                    hs[j], ht[j] = rng.integers(0, n, 2)
+                want = np.empty(nq, np.int32)
+                for gi in (0, 1):
+                    idx = np.where(hg == gi)[0]
+                    rp, col = csrs[gi]
+                    _, w, _ = oracle_mod.stcon_batch(rp, col, hs[idx].copy(), ht[idx].copy(),
+                                                     nthreads=8)
+                    want[idx] = w
+                stats = rep == 2
+                r = fc.stcon_batch(gs, hs, ht, graph_idx=hg, opts=o, out=(hc, hh), stats=stats)
+                assert r[0] is hc and r[1] is hh
+                assert (hh == want).all(), (use_graph, sch, rep)
+                assert (hc == (want >= 0)).all()
+                if stats:
+                    assert r[2]["graph"] == (2 if use_graph else 0)  # captured with the copies
+    # pageable arrays take the copies outside the engine: same answers
+    o = fc.make_opts(sched=fc.SCHED_HEURISTIC, engine=fc.ENGINE_BATCHED, use_graph=1)
+    c2, h2 = fc.stcon_batch(gs, np.array(hs), np.array(ht), graph_idx=np.array(hg), opts=o)
+    assert (h2 == hh).all()
+    for G in gs:
+        G.free()
