@@ -249,14 +249,24 @@ constexpr int MLP_W1 = 0, MLP_B1 = MLP_W1 + MLP_H * MLP_IN, MLP_W2 = MLP_B1 + ML
               MLP_B2 = MLP_W2 + MLP_H * MLP_H, MLP_W3 = MLP_B2 + MLP_H,
               MLP_B3 = MLP_W3 + MLP_OUT * MLP_H, MLP_PARAMS = MLP_B3 + MLP_OUT;
 constexpr int MLP_BOX = MLP_PARAMS, MLP_STORE = MLP_PARAMS + 2 * MLP_IN;
-// The network is consulted only when the heuristic's step would read at
-// least this many adjacency entries: smaller steps cost little whichever way
-// they go, and skipping them keeps the inference off the short-step path.
+// Slack of the trust region in ql_apply_logits (adjacency entries).
 constexpr long long MLP_MIN_EDGES = 1024;
+// The network is consulted only where its answer can change the step: the
+// heuristic's step reads at least MLP_CONSULT_EDGES entries (smaller steps
+// cost little whichever way they go) and the other side's step lies inside
+// the trust region (otherwise the side stays, and the direction and variant
+// heads are not applied against the heuristic's).  On R-MAT 24 batches this
+// cut the learned schedule's time 0.288 -> 0.276 ms (threshold 1,024 and
+// every step consulted before) for 1-2% more entries read.
+constexpr long long MLP_CONSULT_EDGES = 4096;
 
 __host__ __device__ inline bool mlp_worth(const QLocal &q)
 {
-    return (long long)(q.dt[q.side] - q.dh[q.side]) >= MLP_MIN_EDGES;
+    const int x = q.side;
+    const unsigned long long mh = q.dt[x] - q.dh[x];
+    if (!q.two || (long long)mh < MLP_CONSULT_EDGES) return false;
+    const unsigned long long mw = q.dt[1 - x] - q.dh[1 - x];
+    return mw <= 2 * mh + (unsigned long long)MLP_MIN_EDGES;
 }
 static_assert(MLP_PARAMS == 1703, "parameter count");
 
