@@ -89,23 +89,25 @@ int ensure_layout(fc_graph *g, int order, cudaStream_t st)
     return FC_OK;
 }
 
-// The graph an s-t search runs on.  An undirected graph with hubs is searched
-// in its degree-ordered copy: the hubs' status bytes then share a few
-// sectors of each query's status array, which stay in L2, instead of one
-// sector per hub anywhere in it (R-MAT 24, a batch of 1,024 queries: 0.39 ->
-// 0.26 ms).  The kernels map s and t through the copy's id map; answers
+// The graph a search runs on.  An undirected graph with hubs is searched in
+// its degree-ordered copy: the hubs' status bytes then share a few sectors of
+// each query's status array, which stay in L2, instead of one sector per hub
+// anywhere in it (R-MAT 24, a batch of 1,024 queries: 0.39 -> 0.26 ms), and
+// each row lists its highest-degree neighbours first.  The kernels map s and t through the copy's id map; answers
 // (connected, hop distance) do not depend on the numbering.  Directed graphs
 // keep theirs (the copy holds no reverse CSR), and so does the host-loop
-// engine, whose host side reads the ids.  A single query (batch = 0) uses
-// the copy only when asked (FC_ORDER_DEGREE): alone on the GPU its status
-// array stays in L2 anyway, and on the copy the grid's claims crowd the few
-// words that hold the hubs (R-MAT 24: 0.096 -> 0.106 ms per query).  The
-// caller holds the device lock.
-int search_pair(fc_graph *g, const fc_opts &o, int batch, cudaStream_t st, fc::GraphPairH *p)
+// engine, whose host side reads the ids.  by_default = 0 (a single s-t
+// query) uses the copy only when asked (FC_ORDER_DEGREE): alone on the GPU
+// its status array stays in L2 anyway, and on the copy the grid's claims
+// crowd the few words that hold the hubs (R-MAT 24: 0.096 -> 0.106 ms per
+// query); batches and full searches use it by default.  The caller holds
+// the device lock.
+int search_pair(fc_graph *g, const fc_opts &o, int by_default, cudaStream_t st,
+                fc::GraphPairH *p)
 {
     *p = pair_of(g);
     if (g->directed || o.engine == FC_ENGINE_HOSTLOOP) return FC_OK;
-    if (!batch && o.vertex_order != FC_ORDER_DEGREE) return FC_OK;
+    if (!by_default && o.vertex_order != FC_ORDER_DEGREE) return FC_OK;
     int rc = ensure_layout(g, o.vertex_order, st);
     if (rc) return rc;
     if (o.vertex_order != FC_ORDER_GIVEN && g->bfs_layout) {
@@ -540,7 +542,13 @@ int fc_bfs_levels_ex(fc_graph *g, int32_t s, int32_t *levels, const fc_opts *opt
         return fc::engine_bfs_plain(L.c, pair_of(g), lay, s, levels, o, stats,
                                     pick_stream(opts, L.c));
     }
-    return fc::engine_bfs(L.c, pair_of(g), s, levels, o, stats, pick_stream(opts, L.c));
+    // the other schedules search the degree-ordered copy like batches do
+    // (R-MAT 24, direction-optimising: about 1.5 -> 1.1 ms); the levels come
+    // back in the caller's numbering
+    fc::GraphPairH p;
+    int rc = search_pair(g, o, 1, pick_stream(opts, L.c), &p);
+    if (rc) return rc;
+    return fc::engine_bfs(L.c, p, s, levels, o, stats, pick_stream(opts, L.c));
 }
 
 int fc_bfs_trace(int32_t *nlevels, int64_t *level_ns, int64_t *frontier, int64_t *entries,

@@ -751,6 +751,15 @@ static int run_single(DevCtx *c, int mode, int engine, const GraphPairH &gp, int
     return FC_OK;
 }
 
+// Levels of a search on a renumbered copy, back in the caller's numbering:
+// out[v] = lev[remap[v]].
+__global__ void k_levels_to_caller(const int32_t *lev, const int32_t *remap, int nv, int32_t *out)
+{
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < nv;
+         v += (long long)gridDim.x * blockDim.x)
+        out[v] = __ldg(lev + __ldg(remap + v));
+}
+
 int engine_bfs(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_levels, const fc_opts &o,
                fc_stats *st, cudaStream_t stream)
 {
@@ -769,8 +778,15 @@ int engine_bfs(DevCtx *c, const GraphPairH &gp, int32_t s, int32_t *h_levels, co
     }
     if (rc) return rc;
     FC_CUDA_TRY(cudaEventRecord(c->ev1, stream));
+    const int32_t *out = c->levels;
+    if (gp.fwd.remap && h_levels) {  // the log is free once the search is done
+        const int grid = (int)std::min<long long>(4096, ((long long)nv + 255) / 256);
+        k_levels_to_caller<<<grid, 256, 0, stream>>>(c->levels, gp.fwd.remap, nv, c->log);
+        FC_CUDA_TRY(cudaGetLastError());
+        out = c->log;
+    }
     if (h_levels)
-        FC_CUDA_TRY(cudaMemcpyAsync(h_levels, c->levels, sizeof(int32_t) * (size_t)nv,
+        FC_CUDA_TRY(cudaMemcpyAsync(h_levels, out, sizeof(int32_t) * (size_t)nv,
                                     cudaMemcpyDeviceToHost, stream));
     FC_CUDA_TRY(cudaStreamSynchronize(stream));
     if (st) {

@@ -472,6 +472,50 @@ static int grid_for(long long n, int block = IB)
     return (int)g;
 }
 
+int sort_rows_i32(const long long *off, int nv, long long ne, int32_t *col, cudaStream_t st)
+{
+    int *lists = nullptr, *counts = nullptr;
+    int32_t *scratch = nullptr;
+    int h_counts[3] = {0, 0, 0};
+    int rc = FC_OK;
+    auto fail = [&](cudaError_t e, const char *what) {
+        fc_set_last_cuda_error(e, what, __FILE__, __LINE__);
+        rc = e == cudaErrorMemoryAllocation ? FC_ERR_OOM : FC_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&lists, sizeof(int) * (size_t)nv * 3)) != cudaSuccess ||
+        (e = cudaMalloc(&counts, sizeof(int) * 4)) != cudaSuccess ||
+        (e = cudaMemsetAsync(counts, 0, sizeof(int) * 4, st)) != cudaSuccess) {
+        fail(e, "row sort set-up");
+    } else {
+        k_classify<<<(nv + IB - 1) / IB, IB, 0, st>>>(off, nv, lists, counts);
+        if ((e = cudaGetLastError()) != cudaSuccess ||
+            (e = cudaMemcpyAsync(h_counts, counts, sizeof(int) * 3, cudaMemcpyDeviceToHost, st)) !=
+                cudaSuccess ||
+            (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            fail(e, "row classes");
+    }
+    if (rc == FC_OK && h_counts[2] &&
+        (e = cudaMalloc(&scratch, sizeof(int32_t) * (size_t)std::max(1ll, ne))) != cudaSuccess)
+        fail(e, "row sort scratch");
+    if (rc == FC_OK) {
+        if (h_counts[0])
+            k_sort_small<<<grid_for((long long)h_counts[0] * 32), IB, 0, st>>>(off, lists, counts, col);
+        if (h_counts[1])
+            k_sort_medium<<<std::min(h_counts[1], 152 * 8), IB, 0, st>>>(off, lists + (size_t)nv,
+                                                                         counts + 1, col);
+        if (h_counts[2])
+            k_sort_large<<<std::min(h_counts[2], 152 * 4), IB, 0, st>>>(off, lists + 2 * (size_t)nv,
+                                                                        counts + 2, col, scratch);
+        if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaStreamSynchronize(st)) != cudaSuccess)
+            fail(e, "row sort kernels");
+    }
+    cudaFree(lists);
+    cudaFree(counts);
+    cudaFree(scratch);
+    return rc;
+}
+
 int ingest_device_edges(const int32_t *d_src, const int32_t *d_dst, long long n, int nv, int flags,
                         int32_t **out_row_ptr, int32_t **out_col, long long *out_ne,
                         cudaStream_t st)
@@ -480,11 +524,11 @@ int ingest_device_edges(const int32_t *d_src, const int32_t *d_dst, long long n,
     *out_col = nullptr;
     *out_ne = 0;
     if (nv <= 0) return FC_ERR_INVALID;
-    int *deg = nullptr, *bad = nullptr, *lists = nullptr, *counts = nullptr, *ndeg = nullptr;
+    int *deg = nullptr, *bad = nullptr, *ndeg = nullptr;
     long long *off = nullptr, *noff = nullptr;
-    int32_t *tmp = nullptr, *scratch = nullptr, *row_ptr = nullptr, *col = nullptr;
+    int32_t *tmp = nullptr, *row_ptr = nullptr, *col = nullptr;
     int rc = FC_OK;
-    int h_bad = 0, h_counts[3] = {0, 0, 0};
+    int h_bad = 0;
     long long total = 0, ne = 0;
     const int dedupe = !(flags & FC_INGEST_KEEP_DUPS);
 #define ING_TRY(expr)                                                   \
@@ -526,24 +570,8 @@ int ingest_device_edges(const int32_t *d_src, const int32_t *d_dst, long long n,
             ING_TRY(cudaGetLastError());
         }
         // sort rows by size class
-        ING_TRY(cudaMalloc(&lists, sizeof(int) * (size_t)nv * 3));
-        ING_TRY(cudaMalloc(&counts, sizeof(int) * 4));
-        ING_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * 4, st));
-        k_classify<<<(nv + IB - 1) / IB, IB, 0, st>>>(off, nv, lists, counts);
-        ING_TRY(cudaGetLastError());
-        ING_TRY(cudaMemcpyAsync(h_counts, counts, sizeof(int) * 3, cudaMemcpyDeviceToHost, st));
-        ING_TRY(cudaStreamSynchronize(st));
-        if (h_counts[0])
-            k_sort_small<<<grid_for((long long)h_counts[0] * 32), IB, 0, st>>>(off, lists, counts, tmp);
-        if (h_counts[1])
-            k_sort_medium<<<std::min(h_counts[1], 152 * 8), IB, 0, st>>>(off, lists + (size_t)nv,
-                                                                         counts + 1, tmp);
-        if (h_counts[2]) {
-            ING_TRY(cudaMalloc(&scratch, sizeof(int32_t) * (size_t)std::max(1ll, total)));
-            k_sort_large<<<std::min(h_counts[2], 152 * 4), IB, 0, st>>>(off, lists + 2 * (size_t)nv,
-                                                                        counts + 2, tmp, scratch);
-        }
-        ING_TRY(cudaGetLastError());
+        rc = sort_rows_i32(off, nv, total, tmp, st);
+        if (rc) goto done;
         // dedupe: count, scan, compact
         ndeg = deg;  // reuse
         k_count_unique<<<grid_for((long long)nv * 32), IB, 0, st>>>(off, nv, tmp, dedupe, ndeg);
@@ -569,9 +597,6 @@ done:
     cudaFree(off);
     cudaFree(noff);
     cudaFree(tmp);
-    cudaFree(scratch);
-    cudaFree(lists);
-    cudaFree(counts);
     if (rc != FC_OK) {
         cudaFree(row_ptr);
         cudaFree(col);

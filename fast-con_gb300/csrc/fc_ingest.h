@@ -17,6 +17,10 @@ int gen_rmat_device(int scale, long long nedges, double a, double b, double c,
                     unsigned long long seed, long long perm_seed, int32_t *d_src, int32_t *d_dst,
                     cudaStream_t st);
 
+// Sort every row of a CSR with int64 offsets off[0..nv] ascending, in place
+// (ne entries in col).  Waits for the stream.
+int sort_rows_i32(const long long *off, int nv, long long ne, int32_t *col, cudaStream_t st);
+
 // Exclusive scan of n int32 values into out[0..n), out[n] = total (int64).
 int scan_i32(const int32_t *in, long long n, long long *out, cudaStream_t st);
 

@@ -83,22 +83,23 @@ typedef struct fc_opts {
     int32_t private_variant; /* work-sharing engine: expansion variant of the
                              steps an owner CTA runs alone (same codes as
                              `variant`; 0 = the schedule's choice)          */
-    int32_t vertex_order; /* numbering the search runs on, FC_ORDER_*: the
-                             plain BFS engine (FC_ENGINE_AUTO with
-                             FC_SCHED_PLAIN in fc_bfs_levels_ex) and s-t
-                             batches of undirected graphs (not on the
-                             host-loop engine); single s-t queries use the
-                             copy only with FC_ORDER_DEGREE.  Ids in and
-                             levels out are always the caller's.           */
+    int32_t vertex_order; /* numbering the search runs on, FC_ORDER_*: full
+                             BFS (fc_bfs_levels*) and s-t batches of
+                             undirected graphs, except on the host-loop
+                             engine; single s-t queries use the copy only
+                             with FC_ORDER_DEGREE.  Ids in and levels out
+                             are always the caller's.                      */
     int32_t reserved[2];
 } fc_opts;
 
 /* ---- vertex numbering of the searches ------------------------------------ */
-/* The degree-ordered copy (vertices renumbered by descending degree class) is
- * built by the first search that uses it and kept by the graph handle: as
- * much device memory again as the CSR, plus an id map.  It packs the hubs'
- * visited state into a few cache sectors per query slot; a batch of 1,024
- * s-t queries on R-MAT scale 24 runs about a third faster on it. */
+/* The degree-ordered copy (vertices renumbered by descending degree class,
+ * each row listing its highest-degree neighbours first) is built by the first
+ * search that uses it and kept by the graph handle: as much device memory
+ * again as the CSR, plus an id map.  It packs the hubs' visited state into a
+ * few cache sectors per query slot, and searches that stop at the first hit
+ * (the meeting of two sides, a bottom-up parent) stop sooner; a batch of
+ * 1,024 s-t queries on R-MAT scale 24 runs about 40% faster on it. */
 #define FC_ORDER_AUTO   0  /* degree-ordered copy when the graph has hubs
                               (a vertex of degree >= 256), else as given      */
 #define FC_ORDER_GIVEN  1  /* search the caller's numbering                   */
