@@ -69,13 +69,13 @@ typedef struct fc_opts {
     void   *stream;       /* cudaStream_t, NULL = the library's own stream  */
     int32_t cta_work_k;   /* work-sharing engine: a step reading more than
                              cta_work_k * 1024 adjacency entries is cut into
-                             tiles that every CTA may take (0 = 4;
+                             tiles that every CTA may take (0 = 8;
                              < 0 = share every step)                        */
     int32_t variant;      /* top-down expansion variant: 0 = chosen by the
                              schedule, 1 = CTA/warp/scan hybrid, 2 = warp-
                              centric, 3 = one lane per row                  */
     int32_t tile_entries; /* work-sharing engine: a shared top-down tile aims
-                             at this many adjacency entries (0 = 8192 for
+                             at this many adjacency entries (0 = 16384 for
                              batches, 65536 for one query on the grid)      */
     int32_t job_entries;  /* work-sharing engine: rows longer than this are
                              cut into jobs of this length (0 = 2048 for
