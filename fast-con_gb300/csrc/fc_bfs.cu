@@ -19,10 +19,12 @@
 // * Degree-ordered layout.  On graphs with skewed degrees most adjacency
 //   entries of a big level point at a few hub vertices.  The engine keeps,
 //   per graph, a copy of the CSR whose vertices are renumbered by descending
-//   degree (built once, on the first call), so the hubs' visited bits share a
-//   few dozen KB of the bitmap that stay in every SM's L1; on R-MAT 24 the
-//   top 2^18 vertices receive ~85% of the entries of the largest level.  The
-//   levels are mapped back to the caller's numbering in the output pass.
+//   degree (built once, by the first search that uses it; s-t batches and
+//   the other BFS engines use the same copy), so the hubs' visited bits
+//   share a few dozen KB of the bitmap that stay in every SM's L1; on R-MAT
+//   24 the top 2^18 vertices receive ~85% of the entries of the largest
+//   level.  Each row of the copy is sorted by the new ids (its hubs first).
+//   The levels are mapped back to the caller's numbering in the output pass.
 //   Levels do not depend on the numbering.
 //
 // Work per level, with no CTA barrier: each warp takes work from the level's
@@ -49,7 +51,8 @@ namespace fc {
 struct BfsLayout {
     int32_t nv = 0;
     long long ne = 0;
-    int32_t *row_ptr = nullptr;  // renumbered CSR (rows in descending degree class)
+    int32_t *row_ptr = nullptr;  // renumbered CSR (rows in descending degree class,
+                                 // each row's entries ascending: hubs first)
     int32_t *col = nullptr;
     int32_t *new_id = nullptr;   // caller's id -> renumbered id
 };
