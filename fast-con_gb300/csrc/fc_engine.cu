@@ -926,6 +926,8 @@ int engine_stcon_batch(DevCtx *c, const GraphPairH *gps, int ngraphs, const int3
             size_t fit = budget > sstride ? (budget - sstride) / 4 : 0;
             if (fit < log_cap_sz) log_cap_sz = std::max<size_t>(fit, std::min<size_t>(maxnv, 1 << 16));
         }
+        // a caller's cap (at least 1,024 entries) bounds the slots' logs too
+        if (o.slot_log_cap > 0) log_cap_sz = std::min<size_t>(log_cap_sz, std::max(o.slot_log_cap, 1024));
         int log_cap = (int)log_cap_sz;
         rc = ensure_batch_arena(c, (size_t)grid, maxnv, log_cap);
         if (rc) return rc;

@@ -61,7 +61,7 @@ class Opts(ctypes.Structure):
                 ("cta_work_k", ctypes.c_int32), ("variant", ctypes.c_int32),
                 ("tile_entries", ctypes.c_int32), ("job_entries", ctypes.c_int32),
                 ("private_variant", ctypes.c_int32), ("vertex_order", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 2)]
+                ("slot_log_cap", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
 
 
 class Stats(ctypes.Structure):
@@ -167,7 +167,7 @@ def _i32(a):
 
 def make_opts(sched=SCHED_HEURISTIC, engine=ENGINE_AUTO, block=0, ctas_per_sm=0, use_graph=0,
               max_slots=0, stream=None, cta_work_k=0, variant=0, tile_entries=0,
-              job_entries=0, private_variant=0, vertex_order=0) -> Opts:
+              job_entries=0, private_variant=0, vertex_order=0, slot_log_cap=0) -> Opts:
     """variant: 0 = chosen by the schedule, 1 hybrid, 2 warp-centric, 3 lane per row;
     tile_entries / job_entries: work-sharing tile and row-job sizes (0 = defaults);
     vertex_order: numbering the search runs on (ORDER_AUTO / ORDER_GIVEN /
@@ -184,6 +184,7 @@ def make_opts(sched=SCHED_HEURISTIC, engine=ENGINE_AUTO, block=0, ctas_per_sm=0,
     o.tile_entries, o.job_entries = tile_entries, job_entries
     o.private_variant = private_variant
     o.vertex_order = vertex_order
+    o.slot_log_cap = slot_log_cap
     return o
 
 

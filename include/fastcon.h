@@ -89,7 +89,13 @@ typedef struct fc_opts {
                              engine; single s-t queries use the copy only
                              with FC_ORDER_DEGREE.  Ids in and levels out
                              are always the caller's.                      */
-    int32_t reserved[2];
+    int32_t slot_log_cap; /* batches: at most this many entries in each
+                             query slot's visit log (0 = as large as the
+                             arena's memory budget allows, normally one per
+                             vertex).  A query whose claims could outgrow it
+                             is finished by the whole grid afterwards;
+                             smaller logs trade memory for such passes.    */
+    int32_t reserved[1];
 } fc_opts;
 
 /* ---- vertex numbering of the searches ------------------------------------ */

@@ -664,3 +664,31 @@ def test_batch_page_locked_host_arrays(fastcon_lib, oracle_mod):
     assert (h2 == hh).all()
     for G in gs:
         G.free()
+
+
+# --------------------------------------------------------------------------
+# the spill pass: with small query-slot logs, queries whose claims could
+# outgrow their slot are finished by the whole grid after the batch, on the
+# degree-ordered copy and in the caller's numbering, with and without a
+# captured graph
+# --------------------------------------------------------------------------
+def test_batch_spill_pass(fastcon_lib, oracle_mod):
+    fc = fastcon_lib
+    u, v = graphs.rmat_edges(16, 8 << 16, seed=71, perm_seed=72)
+    G = fc.Graph.from_edges(u, v, 1 << 16)
+    rp, col = G.csr()
+    s, t = graphs.pairs_with_degree(np.diff(rp), 600, seed=73)
+    _, want, _ = oracle_mod.stcon_batch(rp, col, s, t, nthreads=16)
+    for order in (fc.ORDER_AUTO, fc.ORDER_GIVEN):
+        for sch in (fc.SCHED_PLAIN, fc.SCHED_HEURISTIC):
+            for ug in (0, 1):
+                o = fc.make_opts(sched=sch, engine=fc.ENGINE_BATCHED, slot_log_cap=1024,
+                                 vertex_order=order, use_graph=ug)
+                conn, hops, st = fc.stcon_batch(G, s, t, opts=o, stats=True)
+                assert (hops == want).all(), (order, sch, ug)
+                assert (conn == (want >= 0)).all()
+                assert st["escalated"] > 0, (order, sch, ug)  # the pass did run
+    # the default (full-size logs) spills nothing
+    conn, hops, st = fc.stcon_batch(G, s, t, opts=fc.make_opts(engine=fc.ENGINE_BATCHED), stats=True)
+    assert (hops == want).all() and st["escalated"] == 0
+    G.free()
