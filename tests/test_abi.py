@@ -59,3 +59,38 @@ def test_opts_layout(fastcon_lib):
     # fc_stats: 2 x int64, 2 x int32, double, int64, 2 x int32, 2 x double,
     # 2 x int64, 2 x int32, int64
     assert ctypes.sizeof(fastcon_lib.Stats) == 16 + 8 + 8 + 8 + 8 + 16 + 16 + 8 + 8
+
+
+def test_struct_offsets_match_the_header(fastcon_lib, tmp_path):
+    """Every field of fc_opts and fc_stats sits where include/fastcon.h puts
+    it: a C program built against the header prints offsetof and sizeof, and
+    the ctypes mirror must agree field by field."""
+    import shutil
+    import subprocess
+
+    import pytest
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    structs = {"fc_opts": fastcon_lib.Opts, "fc_stats": fastcon_lib.Stats}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "fastcon.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "offsets.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "offsets"
+    r = subprocess.run(["gcc", "-std=c11", "-I" + os.path.join(ROOT, "include"), str(src), "-o",
+                        str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        if ln:
+            c, f, v = ln.split()
+            got[(c, f)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "sizeof")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
