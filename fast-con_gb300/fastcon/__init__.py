@@ -173,7 +173,8 @@ def make_opts(sched=SCHED_HEURISTIC, engine=ENGINE_AUTO, block=0, ctas_per_sm=0,
     vertex_order: numbering the search runs on (ORDER_AUTO / ORDER_GIVEN /
     ORDER_DEGREE): the plain BFS engine and s-t batches of undirected graphs
     (single queries only with ORDER_DEGREE); ids in and levels out are always
-    the caller's."""
+    the caller's; slot_log_cap: at most this many entries in each batch query
+    slot's visit log (0 = as large as fits; at least 1,024)."""
     o = Opts()
     lib().fc_opts_init(ctypes.byref(o))
     o.sched, o.engine, o.block, o.ctas_per_sm = sched, engine, block, ctas_per_sm
